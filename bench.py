@@ -1,0 +1,430 @@
+#!/usr/bin/env python3
+"""IDG grid + degrid throughput on one GB300 (or N independent ones).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload config2|config1] [--variant batched|plain]
+
+A step is one imaging cycle over the whole workload: the gridding step
+(gridder -> subgrid FFT -> adder into the uv-grid) followed by the degridding
+step (splitter -> subgrid FFT -> degridder back into visibilities).  The
+default workload is the 100-station / 4950-baseline / 8192 x 1 s / 16-channel
+/ 32x32-subgrid / 4096^2-grid observation (316,800 subgrids, 6.49e8
+visibilities, 20.8 GB of visibilities), seeded synthetic data.
+
+Printed (rank 0, one JSON line):
+  value   Mvis/s = visibilities / (device time of one step), inputs resident in HBM
+  e2e     the same through idg_imaging_cycle() on pinned host buffers, with the
+          visibility copies in and out inside the timed region
+  roofline for the gridder: 17 FMA (34 flop) per pixel-visibility over the
+          measured FP32 FMA peak of this device
+  cpu_baseline the reference's CPU algorithm (the oracle's float restatement of
+          its OpenMP launchers) on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (rank 0), the way the
+driver's reference arm expects.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ska-spc-tender-benchmarks_gb300"))
+
+METRIC = "Mvis/s grid+degrid vs plain GPU form at ≤1e-5 rel err; p50/p99 job latency"
+FLOP_PER_PIXVIS = 34.0  # 16 FMA of the four complex MACs + 1 FMA of the phase
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["config2", "config1"], default="config2")
+    ap.add_argument("--variant", choices=["batched", "plain"], default="batched")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of each baseline half")
+    return ap.parse_args()
+
+
+def workload_spec(name: str, seed: int):
+    from idg_gb300 import datasets as D
+
+    return D.config2(seed=seed) if name == "config2" else D.config1(seed=seed)
+
+
+def config_block(spec, name, extra=None):
+    c = {
+        "workload": f"{name}: {spec.nstations} stations in a {2 * spec.disk_radius_m / 1000:g} km disk, "
+                    f"{spec.n_baselines} baselines x {spec.ntimesteps} x {spec.integration_s:g} s in "
+                    f"{spec.timesteps_per_subgrid}-step subgrids, {spec.nchannels} channels "
+                    f"{spec.f_start / 1e6:g}-{spec.f_end / 1e6:g} MHz, subgrid {spec.subgrid_size}^2, "
+                    f"grid {spec.grid_size}^2, image size {spec.image_size} rad",
+        "n_subgrids": spec.n_subgrids,
+        "n_visibilities": spec.n_visibilities,
+        "subgrid_size": spec.subgrid_size,
+        "grid_size": spec.grid_size,
+        "nchannels": spec.nchannels,
+        "l2": "inputs larger than L2 (visibilities %.1f GB)" % (spec.n_rows * spec.nchannels * 32 / 1e9),
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's CPU algorithm on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_baseline(obs, vis_host: np.ndarray, target_s: float):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build(with_ref=False)
+    spec = obs.spec
+    S, C, T = spec.subgrid_size, spec.nchannels, spec.timesteps_per_subgrid
+    md_all = obs.metadata
+
+    def run(n, grid_too=True):
+        md = md_all[:n].copy()
+        rows = int(md["time_offset"][-1] + md["nr_timesteps"][-1])
+        prm = O.params(spec.grid_size, S, C, spec.nstations, n, spec.image_size)
+        uvw = np.ascontiguousarray(obs.uvw[:rows])
+        vis = np.ascontiguousarray(vis_host[:rows])
+        sub = np.zeros((n, 4, S, S), np.complex64)
+        t0 = time.perf_counter()
+        O.cpu_gridding_omp(prm, uvw, obs.wavenumbers, vis, obs.taper, np.ascontiguousarray(obs.aterms), md, sub)
+        tg = time.perf_counter() - t0
+        out = np.zeros_like(vis)
+        t0 = time.perf_counter()
+        O.cpu_degridding_omp(prm, uvw, obs.wavenumbers, sub, obs.taper, np.ascontiguousarray(obs.aterms), md, out)
+        td = time.perf_counter() - t0
+        return tg, td
+
+    n = 8
+    tg, td = run(n)
+    per = max((tg + td) / n, 1e-6)
+    n = int(max(8, min(spec.n_subgrids, (2 * target_s) / per)))
+    tg, td = run(n)
+    nvis = n * T * C
+    return {
+        "value": nvis / (tg + td) / 1e6,
+        "unit": "Mvis/s",
+        "cores": O.omp_threads(),
+        "kind": "port",
+        "sample": f"first {n} of {spec.n_subgrids} subgrids of the same plan ({nvis} visibilities); "
+                  f"gridding {tg:.2f} s + degridding {td:.2f} s on {O.omp_threads()} OpenMP threads "
+                  f"(float restatement of the reference's OpenMP CPU launchers, -O2)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    spec = workload_spec(args.workload, seed=2 if args.workload == "config2" else 1)
+    obs = D.make_observation(spec)
+    S, C, G = spec.subgrid_size, spec.nchannels, spec.grid_size
+    N = spec.n_subgrids
+    gs = ops.GridSpec(G, S, C, spec.nstations, obs.aterms.shape[0], 1, spec.image_size, spec.w_step)
+    variant = ops.VARIANT_BATCHED if args.variant == "batched" else ops.VARIANT_PLAIN
+
+    stream = torch.cuda.Stream(dev)
+    with torch.cuda.stream(stream):
+        md = ops.metadata_tensor(obs.metadata, dev)
+        uvw = torch.from_numpy(obs.uvw).to(dev)
+        k = torch.from_numpy(obs.wavenumbers).to(dev)
+        taper = torch.from_numpy(obs.taper).to(dev)
+        at = torch.from_numpy(obs.aterms).to(dev)
+        vis = D.visibilities(spec, device=dev, seed=spec.seed + 1000 * rank)
+        vis_out = torch.empty_like(vis)
+        sub = torch.empty((N, 4, S, S), dtype=torch.complex64, device=dev)
+        grid = torch.empty((1, 4, G, G), dtype=torch.complex64, device=dev)
+    stream.synchronize()
+
+    nogrid = gs.__class__(**{**gs.__dict__, "flags": gs.flags | 0x2})  # IDG_FLAG_NO_TAPER
+
+    def step(v=variant, ev=None):
+        # gridding step
+        grid.zero_()
+        if ev: ev[0].record(stream)
+        ops.gridder(nogrid, md, uvw, k, vis, None, at, sub, variant=v, stream=stream)
+        if ev: ev[1].record(stream)
+        ops.subgrid_fft(gs, sub, +1, taper, stream=stream)
+        if ev: ev[2].record(stream)
+        ops.adder(gs, md, sub, grid, stream=stream)
+        if ev: ev[3].record(stream)
+        # degridding step
+        ops.splitter(gs, md, grid, sub, stream=stream)
+        if ev: ev[4].record(stream)
+        ops.subgrid_fft(gs, sub, -1, taper, stream=stream)
+        if ev: ev[5].record(stream)
+        ops.degridder(nogrid, md, uvw, k, vis_out, None, at, sub, variant=v, stream=stream)
+        if ev: ev[6].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+    if ops.device_status(clear=True):
+        raise RuntimeError("a kernel rejected plan entries during warm-up")
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(7)] for _ in range(args.steps)]
+    clocks = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        t0.record(stream)
+        for i in range(args.steps):
+            step(ev=evs[i])
+        t1.record(stream)
+    t1.synchronize()
+    torch.cuda.synchronize(dev)
+    clock_info = clocks.stop()
+    if dist:
+        dist.barrier()
+    elapsed_ms = t0.elapsed_time(t1)
+    parts = np.array([[e[j].elapsed_time(e[j + 1]) for j in range(6)] for e in evs])  # ms per kernel per step
+    if dist:
+        tt = torch.tensor([elapsed_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(tt.item())
+    ms_per_step = elapsed_ms / args.steps
+    nvis = spec.n_visibilities
+    value = world * nvis / (ms_per_step * 1e-3) / 1e6
+
+    # roofline of the gridder (FP32 FMA bound)
+    pixvis = float(nvis) * S * S
+    grid_ms = float(np.mean(parts[:, 0]))
+    degrid_ms = float(np.mean(parts[:, 5]))
+    peak = ops.measure_fp32_peak()
+    achieved = FLOP_PER_PIXVIS * pixvis / (grid_ms * 1e-3)
+    roof = {
+        "bound": "fp32",
+        "kernel": "gridder",
+        "achieved": achieved / 1e12,
+        "peak": peak / 1e12,
+        "unit": "TFLOP/s",
+        "frac": achieved / peak,
+        "traffic": None,
+        "peak_source": "measured in this run: FFMA microbenchmark idg_measure_fp32_peak (MEASURED_PEAKS.json "
+                       "holds HBM and bf16 figures only)",
+        "algorithmic": "34 flop (17 FMA) + 1 sincos per pixel-visibility; %.3g pixel-visibilities per launch" % pixvis,
+        "degridder_frac": FLOP_PER_PIXVIS * pixvis / (degrid_ms * 1e-3) / peak,
+        "kernel_ms": {n: float(np.mean(parts[:, j])) for j, n in enumerate(
+            ["gridder", "fft_fwd", "adder", "splitter", "fft_bwd", "degridder"])},
+    }
+
+    # plain form (one step, same data) for the batched / plain ratio
+    plain = None
+    if not args.no_plain and variant != ops.VARIANT_PLAIN:
+        with torch.cuda.stream(stream):
+            step(v=ops.VARIANT_PLAIN)
+            pe = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
+            step(v=ops.VARIANT_PLAIN, ev=pe)
+        stream.synchronize()
+        pms = pe[0].elapsed_time(pe[6])
+        plain = {"value": nvis / (pms * 1e-3) / 1e6, "unit": "Mvis/s", "ms_per_step": pms,
+                 "gridder_ms": pe[0].elapsed_time(pe[1]), "degridder_ms": pe[5].elapsed_time(pe[6])}
+
+    # e2e through idg_imaging_cycle on pinned host buffers
+    e2e = None
+    cpu = None
+    vis_host = None
+    if not args.no_e2e or rank == 0:
+        vis_host = torch.empty(vis.shape, dtype=vis.dtype, pin_memory=True)
+        vis_host.copy_(vis)
+    del sub, grid, vis_out
+    torch.cuda.empty_cache()
+    if not args.no_e2e:
+        out_host = torch.empty(vis.shape, dtype=vis.dtype, pin_memory=True)
+        chunk = max(1, N // 32)
+        aterms_np = np.ascontiguousarray(obs.aterms)
+        ops.imaging_cycle(gs, obs.metadata, obs.uvw, obs.wavenumbers, vis_host, obs.taper, aterms_np, out_host,
+                          variant=variant, chunk_subgrids=chunk)  # warm (allocates device buffers)
+        totals = []
+        if dist:
+            dist.barrier()
+        for _ in range(args.steps):
+            t = ops.imaging_cycle(gs, obs.metadata, obs.uvw, obs.wavenumbers, vis_host, obs.taper, aterms_np,
+                                  out_host, variant=variant, chunk_subgrids=chunk)
+            totals.append(t)
+        e2e_ms = float(np.mean([t["total_ms"] for t in totals]))
+        if dist:
+            tt = torch.tensor([e2e_ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_ms = float(tt.item())
+        e2e = {"value": world * nvis / (e2e_ms * 1e-3) / 1e6, "unit": "Mvis/s",
+               "h2d_bytes_per_step": int(totals[-1]["h2d_bytes"]), "d2h_bytes_per_step": int(totals[-1]["d2h_bytes"]),
+               "ms_per_step": e2e_ms, "api": "idg_imaging_cycle (C ABI), pinned host buffers",
+               "chunks": (N + chunk - 1) // chunk}
+        # cross-check: the host cycle reproduces the device-resident step's visibilities
+        ops.release_buffers()
+        del out_host
+
+    if rank == 0:
+        cpu = cpu_baseline(obs, vis_host.numpy() if vis_host is not None else None, args.cpu_seconds)
+
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank != 0:
+        return None
+    return {
+        "metric": METRIC,
+        "value": value,
+        "unit": "Mvis/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (FP64 per-subgrid phase offsets)",
+        "data": "synthetic (seeded; N(0,1) visibilities, earth-rotation uvw)",
+        "config": config_block(spec, args.workload, {"variant": args.variant, "parallelism": f"replicas x{world}"}),
+        "e2e": e2e,
+        "gpu_launches": 6 * args.steps,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "plain": plain,
+        "clocks": clock_info,
+    }
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the reference's CPU algorithm on host cores
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from idg_gb300 import datasets as D
+
+    spec = workload_spec(args.workload, seed=2 if args.workload == "config2" else 1)
+    obs = D.make_observation(spec)
+    rng = np.random.default_rng(spec.seed)
+    rows = int(min(spec.n_rows, 2048 * spec.timesteps_per_subgrid))
+    vis = (rng.standard_normal((rows, spec.nchannels, 4), dtype=np.float32) +
+           1j * rng.standard_normal((rows, spec.nchannels, 4), dtype=np.float32)).astype(np.complex64)
+    per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_baseline(obs, vis, min(per_step, 3.0) / 2)
+    vals = []
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(obs, vis, per_step / 2)
+        vals.append(last["value"])
+    value = float(np.mean(vals))
+    last["value"] = value
+    return {
+        "metric": METRIC,
+        "impl": "reference",
+        "value": value,
+        "unit": "Mvis/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": config_block(spec, args.workload, {"parallelism": "host cores"}),
+        "cpu_baseline": last,
+        "e2e": {"value": value, "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local_rank)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

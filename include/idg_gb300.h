@@ -1,0 +1,264 @@
+/*
+ * idg_gb300.h -- C ABI of the GB300 Image-Domain Gridding (IDG) library.
+ *
+ * One process drives one GPU.  All entry points return an idg_status (0 = OK);
+ * idg_last_error() returns the text of the calling thread's last failure.
+ * Device pointers are plain CUDA device addresses; `stream` is a cudaStream_t
+ * passed as void* (NULL = the legacy default stream).  Nothing here takes or
+ * returns a PyTorch type.
+ *
+ * Data layouts (row-major, last index fastest) are those of the reference's
+ * gridding benchmark:
+ *   uvw          [nr_rows][3]                  float (metres)           types.hpp:50-56
+ *   wavenumbers  [nr_channels]                 float (rad / metre)
+ *   visibilities [nr_rows][nr_channels][4]     complex64 (xx, xy, yx, yy) common_gridding.cuh:14-18
+ *   spheroidal   [S][S]                        float (taper)
+ *   aterms       [nr_aterms][nr_stations][S][S][4] complex64               common_gridding.cuh:20-26
+ *   metadata     [nr_subgrids]                 idg_metadata (36 B)       types.hpp:17-25
+ *   subgrids     [nr_subgrids][4][S][S]        complex64                 common_gridding.cuh:7-12
+ *   grid         [nr_w_planes][4][G][G]        complex64                 types.hpp:526-543
+ * A "row" is one (baseline, timestep); metadata.time_offset (minus the first
+ * entry's baseline_offset, plus its own) selects a subgrid's first row
+ * (gridding_benchmark.cpp:61).
+ */
+#ifndef IDG_GB300_H
+#define IDG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define IDG_API __declspec(dllexport)
+#else
+#define IDG_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IDG_ABI_VERSION 1
+
+typedef enum idg_status {
+    IDG_OK = 0,
+    IDG_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, layout or plan entry */
+    IDG_ERR_CUDA = 2,             /* a CUDA runtime call failed (text in idg_last_error) */
+    IDG_ERR_OUT_OF_MEMORY = 3,    /* device or pinned-host allocation failed / over budget */
+    IDG_ERR_UNSUPPORTED = 4,      /* shape outside what the kernels implement */
+    IDG_ERR_TIMEOUT = 5,          /* a bounded wait expired */
+    IDG_ERR_DEVICE_CHECK = 6,     /* a kernel's own bounds check rejected a plan entry */
+    IDG_ERR_NOT_FOUND = 7,        /* unknown job id */
+    IDG_ERR_REJECTED = 8          /* admission control refused a job */
+} idg_status;
+
+/* 36-byte subgrid plan entry: the reference's Metadata, field for field
+ * (gridding/inc/types.hpp:7-25). */
+typedef struct idg_metadata {
+    int32_t baseline_offset;
+    int32_t time_offset;
+    int32_t nr_timesteps;
+    int32_t aterm_index;
+    uint32_t station1;
+    uint32_t station2;
+    int32_t x, y, z;
+} idg_metadata;
+
+/* Per-subgrid sidecar for uneven plans (no counterpart in the reference's
+ * Metadata): the channel range [channel_begin, channel_end) the subgrid
+ * covers.  NULL sidecar = all channels.  Subgrid size is uniform per call. */
+typedef struct idg_subgrid_ext {
+    int32_t channel_begin;
+    int32_t channel_end;
+} idg_subgrid_ext;
+
+/* Flags for idg_params.flags */
+#define IDG_FLAG_DEGRID_ATERM_REFCPU 0x1u /* degridder applies A1^H P A2 (degridding_benchmark.cpp:113)
+                                             instead of the adjoint A1 P A2^H (degridding_benchmark.cu:56) */
+#define IDG_FLAG_NO_TAPER 0x2u            /* gridder/degridder skip the spheroidal (the FFT applies it) */
+
+/* Geometry and physics shared by all kernels of one call. */
+typedef struct idg_params {
+    int32_t grid_size;    /* G */
+    int32_t subgrid_size; /* S (even, 8..64) */
+    int32_t nr_channels;  /* C (1..1024): row length of `visibilities` */
+    int32_t nr_stations;
+    int32_t nr_aterms;    /* leading extent of `aterms` (the reference's ntimeslots) */
+    int32_t nr_w_planes;  /* leading extent of `grid` (>= 1) */
+    float image_size;     /* radians; the reference hard-codes 0.1F (gridding_benchmark.cpp:33) */
+    float w_step;         /* wavelengths; the reference hard-codes 0 (gridding_benchmark.cpp:32) */
+    uint32_t flags;       /* IDG_FLAG_* */
+    int32_t reserved;
+} idg_params;
+
+/* The reference's benchmark_result (gridding/inc/common_gridding.h:5-12):
+ * times in microseconds, bandwidths in bytes per microsecond, -1 = N/A. */
+typedef struct idg_benchmark_result {
+    double in_transfer_time;
+    double out_transfer_time;
+    double in_bandwidth;
+    double out_bandwidth;
+    double compute_time;
+} idg_benchmark_result;
+
+/* Kernel variants */
+#define IDG_VARIANT_PLAIN 0   /* one CTA per subgrid, one sincos per pixel-visibility */
+#define IDG_VARIANT_BATCHED 1 /* persistent CTAs over a cost-sorted work list, TMA-staged inputs */
+
+/* ------------------------------------------------------------------ */
+/* Library                                                            */
+/* ------------------------------------------------------------------ */
+IDG_API int idg_abi_version(void);
+IDG_API const char *idg_last_error(void);
+/* Reads and (if clear != 0) resets the device-side check word of the current
+ * device: bit 0 = a plan entry named rows/stations/A-terms out of range,
+ * bit 1 = a shape the kernel cannot handle.  Synchronises `stream`. */
+IDG_API int idg_device_status(void *stream, uint32_t *status, int clear);
+
+/* ------------------------------------------------------------------ */
+/* Kernels on device-resident data (stream-ordered, asynchronous)      */
+/* ------------------------------------------------------------------ */
+
+/* Gridder: subgrids[s] = taper * (A1^H * sum_{t,c} V[t,c] e^{i phi} * A2).
+ * Replaces kernel_gridder_v7 (gridding/src/gridding_benchmark.cu:231-246) and
+ * the CPU loops of gridding_benchmark.cpp:56-166.  `ext` may be NULL. */
+IDG_API int idg_gridder(const idg_params *params, int variant, int64_t nr_subgrids,
+                        const idg_metadata *metadata, const idg_subgrid_ext *ext, int64_t nr_rows,
+                        const float *uvw, const float *wavenumbers, const void *visibilities,
+                        const float *spheroidal, const void *aterms, void *subgrids, void *stream);
+
+/* Degridder: V[t,c] = sum_pixels A(taper * subgrid) e^{-i phi}; writes only
+ * the rows/channels the plan names.  Replaces kernel_degridder_v6
+ * (gridding/src/degridding_benchmark.cu:106-203) and the CPU loops of
+ * degridding_benchmark.cpp:58-181. */
+IDG_API int idg_degridder(const idg_params *params, int variant, int64_t nr_subgrids,
+                          const idg_metadata *metadata, const idg_subgrid_ext *ext, int64_t nr_rows,
+                          const float *uvw, const float *wavenumbers, void *visibilities,
+                          const float *spheroidal, const void *aterms, const void *subgrids, void *stream);
+
+/* In-place batched subgrid FFT (S in {8,16,24,32,48,64}).
+ * direction +1 (image -> uv, after gridding):
+ *   F[j][i] = sum_{y,x} t P[y][x] exp(+2 pi i((j-S/2)(y-S/2+1/2) + (i-S/2)(x-S/2+1/2))/S)
+ * direction -1 (uv -> image, before degridding): the adjoint, with the taper
+ * applied after the transform.  `taper` may be NULL (t = 1).  No
+ * normalisation: backward(forward(P)) = S^2 P.  No counterpart in the
+ * reference (its upstream ska-sdp-idg-bench holds one; not vendored). */
+IDG_API int idg_subgrid_fft(const idg_params *params, int64_t nr_subgrids, int direction,
+                            const float *taper, void *subgrids, void *stream);
+
+/* Adder: grid[z][pol][y+j][x+i] += F[s][pol][j][i] for cells inside the grid. */
+IDG_API int idg_adder(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                      const void *subgrids, void *grid, void *stream);
+/* Splitter: F[s][pol][j][i] = grid[z][pol][y+j][x+i] (0 outside). */
+IDG_API int idg_splitter(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                         const void *grid, void *subgrids, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* The gridding / degridding steps on device-resident data             */
+/* ------------------------------------------------------------------ */
+/* Gridding step: gridder (no taper) -> subgrid FFT +1 with the taper ->
+ * adder into `grid` (accumulates; zero it first for a fresh image).
+ * `subgrids` is caller-provided work space [nr_subgrids][4][S][S] complex64.
+ * The reference benchmark stops at the gridder; the FFT and adder complete
+ * the step the way its upstream IDG pipeline does. */
+IDG_API int idg_grid_visibilities(const idg_params *params, int variant, int64_t nr_subgrids,
+                                  const idg_metadata *metadata, const idg_subgrid_ext *ext, int64_t nr_rows,
+                                  const float *uvw, const float *wavenumbers, const void *visibilities,
+                                  const float *spheroidal, const void *aterms, void *subgrids, void *grid,
+                                  void *stream);
+/* Degridding step: splitter from `grid` -> subgrid FFT -1 with the taper ->
+ * degridder (no taper) into the rows/channels the plan names. */
+IDG_API int idg_degrid_visibilities(const idg_params *params, int variant, int64_t nr_subgrids,
+                                    const idg_metadata *metadata, const idg_subgrid_ext *ext, int64_t nr_rows,
+                                    const float *uvw, const float *wavenumbers, void *visibilities,
+                                    const float *spheroidal, const void *aterms, void *subgrids, const void *grid,
+                                    void *stream);
+
+/* Timing of one host-buffer imaging cycle (milliseconds, bytes). */
+typedef struct idg_cycle_timing {
+    double total_ms;      /* first host-to-device copy issued .. last device-to-host copy done */
+    double gridding_ms;   /* device time of the gridding phase (gridder + FFT + adder, all chunks) */
+    double degridding_ms; /* device time of the degridding phase (splitter + FFT + degridder) */
+    int64_t h2d_bytes;
+    int64_t d2h_bytes;
+    int64_t kernel_launches;
+} idg_cycle_timing;
+
+/* One imaging cycle on HOST buffers: copies the plan, uvw, wavenumbers,
+ * taper, A-terms and input visibilities in, grids them into a zeroed grid,
+ * degrids the grid back into predicted visibilities and copies those out
+ * (and the grid, if `grid_out` is not NULL).  Visibility copies are cut into
+ * `chunk_subgrids`-subgrid chunks on their own streams so that transfers
+ * overlap the kernels (the plan's rows must then be in chunk order; otherwise
+ * the cycle runs as one chunk).  Device buffers are kept between calls of
+ * the same sizes and freed by idg_release_buffers().  Pinned host buffers
+ * give full copy bandwidth. */
+IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_subgrids,
+                              const idg_metadata *metadata, int64_t nr_rows, const float *uvw,
+                              const float *wavenumbers, const void *visibilities_in, const float *spheroidal,
+                              const void *aterms, void *visibilities_out, void *grid_out, int64_t chunk_subgrids,
+                              idg_cycle_timing *timing);
+IDG_API int idg_release_buffers(void);
+
+/* ------------------------------------------------------------------ */
+/* Drop-in launchers on host data                                      */
+/* ------------------------------------------------------------------ */
+/* The reference's per-call launcher configuration (the fields of
+ * gridding/inc/gridding_configuration.h:54-65 that the launchers read). */
+typedef struct idg_launch_config {
+    int64_t niterations;
+    int64_t grid_size;
+    int64_t subgrid_size;
+    int64_t nstations;
+    int64_t nchannels;
+    int64_t ntimeslots;
+    int64_t ntimesteps_per_subgrid;
+    float image_size; /* 0 = the reference's 0.1F */
+    float w_step;     /* the reference's 0 */
+    uint32_t flags;   /* IDG_FLAG_*; the launchers default to the reference CPU A-term convention
+                         only when IDG_FLAG_DEGRID_ATERM_REFCPU is set */
+    int32_t variant;  /* IDG_VARIANT_* */
+} idg_launch_config;
+
+/* Replaces gridding_benchmark_launcher<hardware_type::gpu>::launch
+ * (gridding/inc/gridding_benchmark.h:10-21, gridding/src/gridding_benchmark.cu:248-361).
+ * Host arrays in the reference's layouts (baselines [n_baselines][2] uint32,
+ * frequencies [C] float, both unused by the kernels, may be NULL).  Copies the
+ * inputs in, grids `niterations` times, copies the subgrids OUT into
+ * `subgrids` (the reference copies them host-to-device at
+ * gridding_benchmark.cu:345, which leaves the host array untouched), and
+ * fills `result` with the reference's timing fields. */
+IDG_API int idg_gridding_launch(const idg_launch_config *config, const float *uvw, const void *visibilities,
+                                const uint32_t *baselines, const void *aterms, const float *frequencies,
+                                const float *wavenumbers, const float *spheroidal, void *subgrids,
+                                const idg_metadata *metadata, idg_benchmark_result *result);
+
+/* Replaces degridding_benchmark_launcher<hardware_type::gpu>::launch
+ * (gridding/inc/degridding_benchmark.h:18-28, gridding/src/degridding_benchmark.cu:205-318).
+ * Copies the subgrids IN (the reference never does, degridding_benchmark.cu:255-264),
+ * degrids, and copies the visibilities OUT into `visibilities`. */
+IDG_API int idg_degridding_launch(const idg_launch_config *config, const float *uvw, void *visibilities,
+                                  const uint32_t *baselines, const void *aterms, const float *frequencies,
+                                  const float *wavenumbers, const float *spheroidal, const void *subgrids,
+                                  const idg_metadata *metadata, idg_benchmark_result *result);
+
+/* ------------------------------------------------------------------ */
+/* Reference-compatible synthetic inputs and plan                     */
+/* ------------------------------------------------------------------ */
+/* Fills host buffers exactly as the reference's launch_gridding does before it
+ * dispatches (srand(0); initialize_uvw, _frequencies, _wavenumbers,
+ * _visibilities, _baselines, _spheroidal, _aterms, _metadata:
+ * gridding/src/gridding_benchmark.cpp:203-213, gridding_initialization.cpp:7-182),
+ * using the C library's rand().  image_size as passed (the reference: 0.1F). */
+IDG_API int idg_reference_dataset(int64_t grid_size, int64_t subgrid_size, int64_t nstations, int64_t nchannels,
+                                  int64_t ntimeslots, int64_t ntimesteps_per_subgrid, float image_size,
+                                  float *uvw, float *frequencies, float *wavenumbers, void *visibilities,
+                                  uint32_t *baselines, float *spheroidal, void *aterms, idg_metadata *metadata);
+
+/* Reports the peak FP32 FMA rate of the current device measured by a short
+ * dependent-chain microbenchmark (flop/s, 2 flop per FMA). */
+IDG_API int idg_measure_fp32_peak(double *flops_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IDG_GB300_H */

@@ -1,0 +1,209 @@
+// idg_fft.cu -- batched subgrid FFT, fused with the taper.
+//
+// direction +1 (image -> uv, after gridding):
+//   F[j][i] = sum_{y,x} t(y,x) P[y][x] exp(+2 pi i((j-S/2)(y-S/2+1/2) + (i-S/2)(x-S/2+1/2))/S)
+// direction -1 (uv -> image, before degridding): the adjoint, taper applied last.
+// For even S this factorises (up to a constant that squares to 1 in 2-D) into
+//   forward : pre-multiply by (-1)^(x+y) t(y,x), unnormalised DFT with e^{+2 pi i jy/S},
+//             post-multiply by c_j c_i,  c_j = (-1)^j e^{+i pi (j-S/2)/S}
+//   backward: pre-multiply by conj(c_j c_i), DFT with e^{-2 pi i jy/S},
+//             post-multiply by (-1)^(x+y) t(y,x)
+// The pixel centres sit half a cell off the DFT lattice (l = (x+1/2-S/2)/S * image_size),
+// which is where the e^{i pi j/S} factors come from.
+//
+// Kernel: a CTA transforms PLANES (subgrid, polarisation) planes.  Planes are
+// loaded with coalesced 8-byte accesses into padded shared memory, one thread
+// per row runs a register-resident radix-2 (x radix-3 for S = 24, 48) FFT,
+// then one thread per column does the same, and the planes are stored back.
+#include "idg_device.cuh"
+#include "idg_internal.h"
+
+namespace idg {
+
+namespace {
+
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
+__host__ __device__ constexpr int bitrev(int i, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+
+// In-register radix-2 DIT FFT of M = 2^k points x[0..M) whose twiddles come
+// from tw[m] = e^{+2 pi i m / N} (M divides N).  SIGN = +1 or -1.
+template <int M, int N, int SIGN>
+__device__ __forceinline__ void fft_pow2(cf *x, const float2 *tw) {
+    constexpr int bits = ilog2(M);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        const int j = bitrev(i, bits);
+        if (j > i) {
+            const cf t = x[i];
+            x[i] = x[j];
+            x[j] = t;
+        }
+    }
+#pragma unroll
+    for (int len = 2; len <= M; len <<= 1) {
+#pragma unroll
+        for (int i0 = 0; i0 < M; i0 += len) {
+#pragma unroll
+            for (int j = 0; j < len / 2; ++j) {
+                const float2 w2 = tw[j * (N / len)];
+                const cf w = {w2.x, SIGN > 0 ? w2.y : -w2.y};
+                const cf u = x[i0 + j];
+                const cf v = (j == 0) ? x[i0 + j + len / 2] : cmul(x[i0 + j + len / 2], w);
+                x[i0 + j] = cadd(u, v);
+                x[i0 + j + len / 2] = {u.re - v.re, u.im - v.im};
+            }
+        }
+    }
+}
+
+// Length-N FFT with N = 2^k or 3 * 2^k, in registers.
+template <int N, int SIGN>
+__device__ __forceinline__ void fft_1d(cf *x, const float2 *tw) {
+    if constexpr ((N & (N - 1)) == 0) {
+        fft_pow2<N, N, SIGN>(x, tw);
+    } else {
+        static_assert(N % 3 == 0 && ((N / 3) & (N / 3 - 1)) == 0, "N must be 2^k or 3*2^k");
+        constexpr int M = N / 3;
+        cf y0[M], y1[M], y2[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            y0[m] = x[3 * m];
+            y1[m] = x[3 * m + 1];
+            y2[m] = x[3 * m + 2];
+        }
+        fft_pow2<M, N, SIGN>(y0, tw);
+        fft_pow2<M, N, SIGN>(y1, tw);
+        fft_pow2<M, N, SIGN>(y2, tw);
+        // omega = e^{SIGN 2 pi i / 3}
+        const float wr = -0.5f, wi = SIGN * 0.86602540378443864676f;
+#pragma unroll
+        for (int k = 0; k < M; ++k) {
+            const float2 t1 = tw[k], t2 = tw[2 * k];
+            const cf w1 = {t1.x, SIGN > 0 ? t1.y : -t1.y}, w2 = {t2.x, SIGN > 0 ? t2.y : -t2.y};
+            const cf a0 = y0[k], a1 = cmul(y1[k], w1), a2 = cmul(y2[k], w2);
+            const cf s = cadd(a1, a2);
+            const cf d = {a1.re - a2.re, a1.im - a2.im};
+            x[k] = cadd(a0, s);
+            // a0 + omega a1 + omega^2 a2 = a0 - s/2 + i*wi*d ; the third output uses -i*wi*d
+            const cf base = {a0.re + wr * s.re, a0.im + wr * s.im};
+            x[k + M] = {base.re - wi * d.im, base.im + wi * d.re};
+            x[k + 2 * M] = {base.re + wi * d.im, base.im - wi * d.re};
+        }
+    }
+}
+
+template <int S>
+struct FftShape {
+    static constexpr int planes = S >= 64 ? 1 : 128 / S; // <= 48 KiB of static shared memory
+    static constexpr int threads = planes * S;
+    static constexpr int pitch = S + 1; // float2 per padded row
+};
+
+template <int S, int DIR>
+__global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float2 *data, int64_t nr_planes,
+                                                                          const float *taper) {
+    using Sh = FftShape<S>;
+    __shared__ float2 tw[S];      // e^{+2 pi i m / S}
+    __shared__ float2 post[S];    // c_j = (-1)^j e^{+i pi (j - S/2)/S}
+    __shared__ float2 buf[Sh::planes][S][Sh::pitch];
+
+    const int tid = threadIdx.x;
+    if (tid < S) {
+        double s, c;
+        sincospi(2.0 * tid / S, &s, &c);
+        tw[tid] = make_float2((float)c, (float)s);
+        sincospi((tid - S * 0.5) / S, &s, &c);
+        const double sg = (tid & 1) ? -1.0 : 1.0;
+        post[tid] = make_float2((float)(sg * c), (float)(sg * s));
+    }
+    const int64_t plane0 = (int64_t)blockIdx.x * Sh::planes;
+    const int nplanes = (int)min((int64_t)Sh::planes, nr_planes - plane0);
+    __syncthreads();
+
+    // load + pre-multiply
+    for (int e = tid; e < nplanes * S * S; e += Sh::threads) {
+        const int pl = e / (S * S), q = e - pl * S * S, y = q / S, x = q - y * S;
+        float2 v = data[(plane0 + pl) * S * S + q];
+        if (DIR > 0) {
+            const float f = (((x + y) & 1) ? -1.f : 1.f) * (taper ? taper[q] : 1.f);
+            v = make_float2(v.x * f, v.y * f);
+        } else {
+            const float2 cy = post[y], cx = post[x];
+            const cf w = cconj(cmul({cy.x, cy.y}, {cx.x, cx.y}));
+            const cf r = cmul({v.x, v.y}, w);
+            v = make_float2(r.re, r.im);
+        }
+        buf[pl][y][x] = v;
+    }
+    __syncthreads();
+
+    const int pl = tid / S, r = tid - (tid / S) * S;
+    cf x[S];
+    if (pl < nplanes) {
+#pragma unroll
+        for (int i = 0; i < S; ++i) x[i] = {buf[pl][r][i].x, buf[pl][r][i].y};
+        fft_1d<S, DIR>(x, tw);
+#pragma unroll
+        for (int i = 0; i < S; ++i) buf[pl][r][i] = make_float2(x[i].re, x[i].im);
+    }
+    __syncthreads();
+    if (pl < nplanes) {
+#pragma unroll
+        for (int i = 0; i < S; ++i) x[i] = {buf[pl][i][r].x, buf[pl][i][r].y};
+        fft_1d<S, DIR>(x, tw);
+#pragma unroll
+        for (int i = 0; i < S; ++i) buf[pl][i][r] = make_float2(x[i].re, x[i].im);
+    }
+    __syncthreads();
+
+    // post-multiply + store
+    for (int e = tid; e < nplanes * S * S; e += Sh::threads) {
+        const int pl2 = e / (S * S), q = e - pl2 * S * S, y = q / S, xx = q - y * S;
+        float2 v = buf[pl2][y][xx];
+        if (DIR > 0) {
+            const float2 cy = post[y], cx = post[xx];
+            const cf r2 = cmul(cmul({v.x, v.y}, {cy.x, cy.y}), {cx.x, cx.y});
+            v = make_float2(r2.re, r2.im);
+        } else {
+            const float f = (((xx + y) & 1) ? -1.f : 1.f) * (taper ? taper[q] : 1.f);
+            v = make_float2(v.x * f, v.y * f);
+        }
+        data[(plane0 + pl2) * S * S + q] = v;
+    }
+}
+
+template <int S>
+cudaError_t launch_fft_s(float2 *data, int64_t nr_planes, int direction, const float *taper, cudaStream_t stream) {
+    using Sh = FftShape<S>;
+    const int64_t blocks = (nr_planes + Sh::planes - 1) / Sh::planes;
+    if (blocks == 0) return cudaSuccess;
+    if (direction > 0)
+        subgrid_fft_kernel<S, 1><<<(unsigned)blocks, Sh::threads, 0, stream>>>(data, nr_planes, taper);
+    else
+        subgrid_fft_kernel<S, -1><<<(unsigned)blocks, Sh::threads, 0, stream>>>(data, nr_planes, taper);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+bool fft_size_supported(int S) { return S == 8 || S == 16 || S == 24 || S == 32 || S == 48 || S == 64; }
+
+cudaError_t launch_subgrid_fft(float2 *data, int64_t nr_subgrids, int S, int direction, const float *taper,
+                               cudaStream_t stream) {
+    const int64_t planes = nr_subgrids * 4;
+    switch (S) {
+    case 8: return launch_fft_s<8>(data, planes, direction, taper, stream);
+    case 16: return launch_fft_s<16>(data, planes, direction, taper, stream);
+    case 24: return launch_fft_s<24>(data, planes, direction, taper, stream);
+    case 32: return launch_fft_s<32>(data, planes, direction, taper, stream);
+    case 48: return launch_fft_s<48>(data, planes, direction, taper, stream);
+    case 64: return launch_fft_s<64>(data, planes, direction, taper, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+} // namespace idg

@@ -1,0 +1,25 @@
+// idg_internal.h -- launch functions shared between the kernel files and the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace idg {
+
+struct KernelArgs;
+
+cudaError_t launch_gridder(const KernelArgs &a, int variant, int max_nc, cudaStream_t stream);
+cudaError_t launch_degridder(const KernelArgs &a, int variant, int max_nc, cudaStream_t stream);
+
+bool fft_size_supported(int S);
+cudaError_t launch_subgrid_fft(float2 *data, int64_t nr_subgrids, int S, int direction, const float *taper,
+                               cudaStream_t stream);
+
+cudaError_t launch_adder(const struct idg_metadata *md, int64_t nr_subgrids, int S, int G, int W,
+                         const float2 *subgrids, float2 *grid, cudaStream_t stream);
+cudaError_t launch_splitter(const struct idg_metadata *md, int64_t nr_subgrids, int S, int G, int W,
+                            const float2 *grid, float2 *subgrids, cudaStream_t stream);
+
+cudaError_t measure_fp32_peak(double *flops);
+
+} // namespace idg

@@ -1,0 +1,286 @@
+// idg_pipeline.cu -- the gridding and degridding steps, and the host-buffer
+// imaging cycle with copy/compute overlap.
+//
+// Gridding step   : gridder (taper off) -> subgrid FFT +1 (taper fused) -> adder
+// Degridding step : splitter -> subgrid FFT -1 (taper fused) -> degridder (taper off)
+// The taper moves from the gridder epilogue / degridder prologue into the
+// FFT's pre/post multiplication, where it costs nothing extra.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "idg_device.cuh"
+#include "idg_host.h"
+#include "idg_internal.h"
+
+using namespace idg;
+
+namespace {
+
+int check_step_args(const idg_params *params, int64_t nr_subgrids, const void *subgrids, const void *grid) {
+    if (int rc = check_params(params, true)) return rc;
+    if (nr_subgrids < 0) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_subgrids < 0");
+    if (nr_subgrids > 0 && (!subgrids || !grid)) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL subgrids or grid");
+    return IDG_OK;
+}
+
+// Device buffers of the host-buffer cycle, kept between calls.
+struct CycleBuffers {
+    int device = -1;
+    void *uvw = nullptr, *k = nullptr, *taper = nullptr, *aterms = nullptr, *md = nullptr;
+    void *vis_in = nullptr, *vis_out = nullptr, *subgrids = nullptr, *grid = nullptr;
+    size_t b_uvw = 0, b_k = 0, b_taper = 0, b_aterms = 0, b_md = 0, b_vis = 0, b_vis_out = 0, b_sub = 0, b_grid = 0;
+    cudaStream_t s_compute = nullptr, s_h2d = nullptr, s_d2h = nullptr;
+
+    void release() {
+        for (void *p : {uvw, k, taper, aterms, md, vis_in, vis_out, subgrids, grid})
+            if (p) cudaFree(p);
+        uvw = k = taper = aterms = md = vis_in = vis_out = subgrids = grid = nullptr;
+        b_uvw = b_k = b_taper = b_aterms = b_md = b_vis = b_vis_out = b_sub = b_grid = 0;
+        for (cudaStream_t s : {s_compute, s_h2d, s_d2h})
+            if (s) cudaStreamDestroy(s);
+        s_compute = s_h2d = s_d2h = nullptr;
+        device = -1;
+    }
+};
+std::mutex g_cycle_mutex;
+CycleBuffers g_cycle;
+
+int ensure(void **p, size_t *have, size_t want) {
+    if (want == 0) want = 16;
+    if (*p && *have >= want) return IDG_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    IDG_CUDA(cudaMalloc(p, want));
+    *have = want;
+    return IDG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+IDG_API int idg_grid_visibilities(const idg_params *params, int variant, int64_t nr_subgrids,
+                                  const idg_metadata *metadata, const idg_subgrid_ext *ext, int64_t nr_rows,
+                                  const float *uvw, const float *wavenumbers, const void *visibilities,
+                                  const float *spheroidal, const void *aterms, void *subgrids, void *grid,
+                                  void *stream) {
+    if (int rc = check_step_args(params, nr_subgrids, subgrids, grid)) return rc;
+    if (nr_subgrids == 0) return IDG_OK;
+    idg_params p = *params;
+    p.flags |= IDG_FLAG_NO_TAPER;
+    if (int rc = idg_gridder(&p, variant, nr_subgrids, metadata, ext, nr_rows, uvw, wavenumbers, visibilities,
+                             nullptr, aterms, subgrids, stream))
+        return rc;
+    if (int rc = idg_subgrid_fft(params, nr_subgrids, +1, spheroidal, subgrids, stream)) return rc;
+    return idg_adder(params, nr_subgrids, metadata, subgrids, grid, stream);
+}
+
+IDG_API int idg_degrid_visibilities(const idg_params *params, int variant, int64_t nr_subgrids,
+                                    const idg_metadata *metadata, const idg_subgrid_ext *ext, int64_t nr_rows,
+                                    const float *uvw, const float *wavenumbers, void *visibilities,
+                                    const float *spheroidal, const void *aterms, void *subgrids, const void *grid,
+                                    void *stream) {
+    if (int rc = check_step_args(params, nr_subgrids, subgrids, grid)) return rc;
+    if (nr_subgrids == 0) return IDG_OK;
+    if (int rc = idg_splitter(params, nr_subgrids, metadata, grid, subgrids, stream)) return rc;
+    if (int rc = idg_subgrid_fft(params, nr_subgrids, -1, spheroidal, subgrids, stream)) return rc;
+    idg_params p = *params;
+    p.flags |= IDG_FLAG_NO_TAPER;
+    return idg_degridder(&p, variant, nr_subgrids, metadata, ext, nr_rows, uvw, wavenumbers, visibilities, nullptr,
+                         aterms, subgrids, stream);
+}
+
+IDG_API int idg_release_buffers(void) {
+    std::lock_guard<std::mutex> lock(g_cycle_mutex);
+    g_cycle.release();
+    return IDG_OK;
+}
+
+IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_subgrids,
+                              const idg_metadata *metadata, int64_t nr_rows, const float *uvw,
+                              const float *wavenumbers, const void *visibilities_in, const float *spheroidal,
+                              const void *aterms, void *visibilities_out, void *grid_out, int64_t chunk_subgrids,
+                              idg_cycle_timing *timing) {
+    if (int rc = check_params(params, true)) return rc;
+    if (nr_subgrids < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_subgrids < 1");
+    if (nr_rows < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_rows < 1");
+    if (!metadata || !uvw || !wavenumbers || !visibilities_in || !spheroidal || !aterms || !visibilities_out)
+        return fail(IDG_ERR_INVALID_ARGUMENT, "NULL host array");
+    const int64_t S = params->subgrid_size, C = params->nr_channels, G = params->grid_size;
+    const int64_t W = params->nr_w_planes > 0 ? params->nr_w_planes : 1;
+
+    // chunk row ranges; rows must advance chunk by chunk to overlap copies
+    if (chunk_subgrids < 1 || chunk_subgrids > nr_subgrids) chunk_subgrids = nr_subgrids;
+    const int bo1 = metadata[0].baseline_offset;
+    std::vector<int64_t> c_begin, c_rows0, c_rows1;
+    int64_t prev_end = 0;
+    bool ordered = true;
+    for (int64_t s0 = 0; s0 < nr_subgrids; s0 += chunk_subgrids) {
+        const int64_t s1 = std::min(nr_subgrids, s0 + chunk_subgrids);
+        int64_t r0 = INT64_MAX, r1 = 0;
+        for (int64_t s = s0; s < s1; ++s) {
+            const idg_metadata &m = metadata[s];
+            const int64_t a = (int64_t)(m.baseline_offset - bo1) + m.time_offset;
+            if (a < 0 || m.nr_timesteps < 0 || a + m.nr_timesteps > nr_rows)
+                return fail(IDG_ERR_INVALID_ARGUMENT, "plan entry %lld names rows outside [0, %lld)", (long long)s,
+                            (long long)nr_rows);
+            r0 = std::min(r0, a);
+            r1 = std::max(r1, a + m.nr_timesteps);
+        }
+        if (r0 < prev_end) ordered = false;
+        prev_end = r1;
+        c_begin.push_back(s0);
+        c_rows0.push_back(r0);
+        c_rows1.push_back(r1);
+    }
+    if (!ordered) {
+        c_begin.assign(1, 0);
+        c_rows0.assign(1, 0);
+        c_rows1.assign(1, nr_rows);
+    }
+    c_begin.push_back(nr_subgrids);
+    const size_t nchunks = c_rows0.size();
+
+    std::lock_guard<std::mutex> lock(g_cycle_mutex);
+    CycleBuffers &B = g_cycle;
+    int dev = 0;
+    IDG_CUDA(cudaGetDevice(&dev));
+    if (B.device != dev) {
+        B.release();
+        B.device = dev;
+    }
+    if (!B.s_compute) {
+        IDG_CUDA(cudaStreamCreateWithFlags(&B.s_compute, cudaStreamNonBlocking));
+        IDG_CUDA(cudaStreamCreateWithFlags(&B.s_h2d, cudaStreamNonBlocking));
+        IDG_CUDA(cudaStreamCreateWithFlags(&B.s_d2h, cudaStreamNonBlocking));
+    }
+    const size_t b_uvw = (size_t)nr_rows * 12, b_k = (size_t)C * 4, b_taper = (size_t)S * S * 4,
+                 b_aterms = (size_t)params->nr_aterms * params->nr_stations * S * S * 32,
+                 b_md = (size_t)nr_subgrids * sizeof(idg_metadata), b_vis = (size_t)nr_rows * C * 32,
+                 b_sub = (size_t)nr_subgrids * 4 * S * S * 8, b_grid = (size_t)W * 4 * G * G * 8;
+    if (int rc = ensure(&B.uvw, &B.b_uvw, b_uvw)) return rc;
+    if (int rc = ensure(&B.k, &B.b_k, b_k)) return rc;
+    if (int rc = ensure(&B.taper, &B.b_taper, b_taper)) return rc;
+    if (int rc = ensure(&B.aterms, &B.b_aterms, b_aterms)) return rc;
+    if (int rc = ensure(&B.md, &B.b_md, b_md)) return rc;
+    if (int rc = ensure(&B.vis_in, &B.b_vis, b_vis)) return rc;
+    if (int rc = ensure(&B.vis_out, &B.b_vis_out, b_vis)) return rc;
+    if (int rc = ensure(&B.subgrids, &B.b_sub, b_sub)) return rc;
+    if (int rc = ensure(&B.grid, &B.b_grid, b_grid)) return rc;
+
+    std::vector<cudaEvent_t> ev;
+    auto new_event = [&](cudaEvent_t *e, bool timing_event) -> int {
+        IDG_CUDA(cudaEventCreateWithFlags(e, timing_event ? cudaEventDefault : cudaEventDisableTiming));
+        ev.push_back(*e);
+        return IDG_OK;
+    };
+    struct EventGuard {
+        std::vector<cudaEvent_t> &v;
+        ~EventGuard() {
+            for (cudaEvent_t e : v) cudaEventDestroy(e);
+        }
+    } guard{ev};
+
+    cudaEvent_t t_start, t_grid0, t_grid1, t_deg1, t_end, consts_in;
+    if (int rc = new_event(&t_start, true)) return rc;
+    if (int rc = new_event(&t_grid0, true)) return rc;
+    if (int rc = new_event(&t_grid1, true)) return rc;
+    if (int rc = new_event(&t_deg1, true)) return rc;
+    if (int rc = new_event(&t_end, true)) return rc;
+    if (int rc = new_event(&consts_in, false)) return rc;
+    std::vector<cudaEvent_t> h2d_done(nchunks), deg_done(nchunks);
+    for (size_t i = 0; i < nchunks; ++i) {
+        if (int rc = new_event(&h2d_done[i], false)) return rc;
+        if (int rc = new_event(&deg_done[i], false)) return rc;
+    }
+
+    IDG_CUDA(cudaDeviceSynchronize());
+    int64_t launches = 0, h2d = 0, d2h = 0;
+    IDG_CUDA(cudaEventRecord(t_start, B.s_h2d));
+    // constants first (small), then visibility chunks
+    IDG_CUDA(cudaMemcpyAsync(B.md, metadata, b_md, cudaMemcpyHostToDevice, B.s_h2d));
+    IDG_CUDA(cudaMemcpyAsync(B.uvw, uvw, b_uvw, cudaMemcpyHostToDevice, B.s_h2d));
+    IDG_CUDA(cudaMemcpyAsync(B.k, wavenumbers, b_k, cudaMemcpyHostToDevice, B.s_h2d));
+    IDG_CUDA(cudaMemcpyAsync(B.taper, spheroidal, b_taper, cudaMemcpyHostToDevice, B.s_h2d));
+    IDG_CUDA(cudaMemcpyAsync(B.aterms, aterms, b_aterms, cudaMemcpyHostToDevice, B.s_h2d));
+    h2d += b_md + b_uvw + b_k + b_taper + b_aterms;
+    IDG_CUDA(cudaEventRecord(consts_in, B.s_h2d));
+    for (size_t i = 0; i < nchunks; ++i) {
+        const size_t off = (size_t)c_rows0[i] * C * 32, bytes = (size_t)(c_rows1[i] - c_rows0[i]) * C * 32;
+        IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.vis_in) + off, static_cast<const char *>(visibilities_in) + off,
+                                 bytes, cudaMemcpyHostToDevice, B.s_h2d));
+        h2d += bytes;
+        IDG_CUDA(cudaEventRecord(h2d_done[i], B.s_h2d));
+    }
+
+    // gridding phase
+    IDG_CUDA(cudaStreamWaitEvent(B.s_compute, consts_in, 0));
+    IDG_CUDA(cudaMemsetAsync(B.grid, 0, b_grid, B.s_compute));
+    IDG_CUDA(cudaEventRecord(t_grid0, B.s_compute));
+    const idg_metadata *d_md = static_cast<const idg_metadata *>(B.md);
+    for (size_t i = 0; i < nchunks; ++i) {
+        IDG_CUDA(cudaStreamWaitEvent(B.s_compute, h2d_done[i], 0));
+        const int64_t s0 = c_begin[i], n = c_begin[i + 1] - s0;
+        if (int rc = idg_grid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,
+                                           (const float *)B.k, B.vis_in, (const float *)B.taper, B.aterms,
+                                           static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
+                                           B.s_compute))
+            return rc;
+        launches += 3;
+    }
+    IDG_CUDA(cudaEventRecord(t_grid1, B.s_compute));
+
+    // degridding phase (rows the plan does not name come back as zeros)
+    IDG_CUDA(cudaMemsetAsync(B.vis_out, 0, b_vis, B.s_compute));
+    for (size_t i = 0; i < nchunks; ++i) {
+        const int64_t s0 = c_begin[i], n = c_begin[i + 1] - s0;
+        if (int rc = idg_degrid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,
+                                             (const float *)B.k, B.vis_out, (const float *)B.taper, B.aterms,
+                                             static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
+                                             B.s_compute))
+            return rc;
+        launches += 3;
+        IDG_CUDA(cudaEventRecord(deg_done[i], B.s_compute));
+        IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, deg_done[i], 0));
+        const size_t off = (size_t)c_rows0[i] * C * 32, bytes = (size_t)(c_rows1[i] - c_rows0[i]) * C * 32;
+        IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(visibilities_out) + off, static_cast<char *>(B.vis_out) + off,
+                                 bytes, cudaMemcpyDeviceToHost, B.s_d2h));
+        d2h += bytes;
+    }
+    IDG_CUDA(cudaEventRecord(t_deg1, B.s_compute));
+    if (grid_out) {
+        IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, t_grid1, 0));
+        IDG_CUDA(cudaMemcpyAsync(grid_out, B.grid, b_grid, cudaMemcpyDeviceToHost, B.s_d2h));
+        d2h += b_grid;
+    }
+    IDG_CUDA(cudaEventRecord(t_end, B.s_d2h));
+    IDG_CUDA(cudaEventSynchronize(t_end));
+    IDG_CUDA(cudaStreamSynchronize(B.s_compute));
+
+    DeviceWords w;
+    if (int rc = device_words(&w)) return rc;
+    unsigned status = 0;
+    IDG_CUDA(cudaMemcpy(&status, w.status, sizeof status, cudaMemcpyDeviceToHost));
+    if (status) {
+        IDG_CUDA(cudaMemset(w.status, 0, sizeof(unsigned)));
+        return fail(IDG_ERR_DEVICE_CHECK, "a kernel rejected plan entries (status 0x%x)", status);
+    }
+    if (timing) {
+        float total = 0, g = 0, d = 0;
+        IDG_CUDA(cudaEventElapsedTime(&total, t_start, t_end));
+        IDG_CUDA(cudaEventElapsedTime(&g, t_grid0, t_grid1));
+        IDG_CUDA(cudaEventElapsedTime(&d, t_grid1, t_deg1));
+        timing->total_ms = total;
+        timing->gridding_ms = g;
+        timing->degridding_ms = d;
+        timing->h2d_bytes = h2d;
+        timing->d2h_bytes = d2h;
+        timing->kernel_launches = launches;
+    }
+    return IDG_OK;
+}
+
+} // extern "C"

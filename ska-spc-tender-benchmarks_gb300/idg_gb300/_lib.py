@@ -1,0 +1,196 @@
+"""ctypes binding of ``libidg_gb300.so`` (declarations in include/idg_gb300.h).
+
+The library is the only compute path: there is no Python or PyTorch
+fallback.  If it is missing it is built in-tree on first use; if it cannot be
+built or loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+IDG_OK = 0
+IDG_ERR_INVALID_ARGUMENT = 1
+IDG_ERR_CUDA = 2
+IDG_ERR_OUT_OF_MEMORY = 3
+IDG_ERR_UNSUPPORTED = 4
+IDG_ERR_TIMEOUT = 5
+IDG_ERR_DEVICE_CHECK = 6
+IDG_ERR_NOT_FOUND = 7
+IDG_ERR_REJECTED = 8
+
+IDG_FLAG_DEGRID_ATERM_REFCPU = 0x1
+IDG_FLAG_NO_TAPER = 0x2
+
+VARIANT_PLAIN = 0
+VARIANT_BATCHED = 1
+
+# 36-byte plan entry (gridding/inc/types.hpp:17-25)
+METADATA_DTYPE = np.dtype(
+    [
+        ("baseline_offset", "<i4"),
+        ("time_offset", "<i4"),
+        ("nr_timesteps", "<i4"),
+        ("aterm_index", "<i4"),
+        ("station1", "<u4"),
+        ("station2", "<u4"),
+        ("x", "<i4"),
+        ("y", "<i4"),
+        ("z", "<i4"),
+    ]
+)
+SUBGRID_EXT_DTYPE = np.dtype([("channel_begin", "<i4"), ("channel_end", "<i4")])
+
+
+class IdgParams(ctypes.Structure):
+    _fields_ = [
+        ("grid_size", ctypes.c_int32),
+        ("subgrid_size", ctypes.c_int32),
+        ("nr_channels", ctypes.c_int32),
+        ("nr_stations", ctypes.c_int32),
+        ("nr_aterms", ctypes.c_int32),
+        ("nr_w_planes", ctypes.c_int32),
+        ("image_size", ctypes.c_float),
+        ("w_step", ctypes.c_float),
+        ("flags", ctypes.c_uint32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class IdgBenchmarkResult(ctypes.Structure):
+    _fields_ = [
+        ("in_transfer_time", ctypes.c_double),
+        ("out_transfer_time", ctypes.c_double),
+        ("in_bandwidth", ctypes.c_double),
+        ("out_bandwidth", ctypes.c_double),
+        ("compute_time", ctypes.c_double),
+    ]
+
+
+class IdgCycleTiming(ctypes.Structure):
+    _fields_ = [
+        ("total_ms", ctypes.c_double),
+        ("gridding_ms", ctypes.c_double),
+        ("degridding_ms", ctypes.c_double),
+        ("h2d_bytes", ctypes.c_int64),
+        ("d2h_bytes", ctypes.c_int64),
+        ("kernel_launches", ctypes.c_int64),
+    ]
+
+
+class IdgLaunchConfig(ctypes.Structure):
+    _fields_ = [
+        ("niterations", ctypes.c_int64),
+        ("grid_size", ctypes.c_int64),
+        ("subgrid_size", ctypes.c_int64),
+        ("nstations", ctypes.c_int64),
+        ("nchannels", ctypes.c_int64),
+        ("ntimeslots", ctypes.c_int64),
+        ("ntimesteps_per_subgrid", ctypes.c_int64),
+        ("image_size", ctypes.c_float),
+        ("w_step", ctypes.c_float),
+        ("flags", ctypes.c_uint32),
+        ("variant", ctypes.c_int32),
+    ]
+
+
+class IdgError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"idg error {code}: {message}")
+        self.code = code
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int
+
+# name -> argtypes (all entry points return int status unless listed in _RESTYPES)
+_SIGNATURES = {
+    "idg_abi_version": [],
+    "idg_last_error": [],
+    "idg_device_status": [_P, ctypes.POINTER(ctypes.c_uint32), _I32],
+    "idg_gridder": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
+    "idg_degridder": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
+    "idg_subgrid_fft": [ctypes.POINTER(IdgParams), _I64, _I32, _P, _P, _P],
+    "idg_adder": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
+    "idg_splitter": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
+    "idg_grid_visibilities": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P],
+    "idg_degrid_visibilities": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P],
+    "idg_imaging_cycle": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64,
+                          ctypes.c_void_p],
+    "idg_release_buffers": [],
+    "idg_gridding_launch": [ctypes.POINTER(IdgLaunchConfig), _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                            ctypes.POINTER(IdgBenchmarkResult)],
+    "idg_degridding_launch": [ctypes.POINTER(IdgLaunchConfig), _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                              ctypes.POINTER(IdgBenchmarkResult)],
+    "idg_reference_dataset": [_I64, _I64, _I64, _I64, _I64, _I64, ctypes.c_float, _P, _P, _P, _P, _P, _P, _P, _P],
+    "idg_measure_fp32_peak": [ctypes.POINTER(ctypes.c_double)],
+}
+_RESTYPES = {"idg_last_error": ctypes.c_char_p, "idg_abi_version": ctypes.c_int}
+
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load (building first if needed) the native library; raises if impossible."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB_PATH
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise IdgError(IDG_ERR_UNSUPPORTED, f"{path} is missing and building was not requested")
+            _build.build()
+        lib = ctypes.CDLL(path)
+        for name, argtypes in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = argtypes
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        _lib = lib
+        return lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+def last_error() -> str:
+    msg = load().idg_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc: int) -> None:
+    if rc != IDG_OK:
+        raise IdgError(rc, last_error())
+
+
+def call(name: str, *args) -> None:
+    check(getattr(load(), name)(*args))
+
+
+def ptr(x) -> int | None:
+    """Raw address of a torch tensor (device or host) or numpy array; None for None."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return x.data_ptr()
+    if isinstance(x, int):
+        return x
+    raise TypeError(f"cannot take the address of {type(x)}")

@@ -1,0 +1,235 @@
+"""Seeded synthetic observations and the uvw-driven subgrid plan.
+
+No public data set is involved: every input is generated from a seed.
+
+Observation model (all lengths in metres, angles in radians):
+
+* ``nstations`` stations uniform in a disk of radius ``disk_radius_m``
+  (east, north, up=0), all ``nstations*(nstations-1)/2`` baselines.
+* Earth-rotation synthesis for a source at declination ``dec`` seen from
+  latitude ``lat``: local (E, N, U) -> equatorial (X, Y, Z) with
+  X = -sin(lat) N + cos(lat) U, Y = E, Z = cos(lat) N + sin(lat) U, then for
+  hour angle H
+      u =  sin H X + cos H Y
+      v = -sin dec cos H X + sin dec sin H Y + cos dec Z
+      w =  cos dec cos H X - cos dec sin H Y + sin dec Z
+  with H advancing 7.2921159e-5 rad per second over ``ntimesteps`` integrations
+  of ``integration_s`` seconds, centred on transit.
+* ``nchannels`` channels linearly spaced from ``f_start`` to ``f_end``;
+  wavenumbers k = 2 pi f / c in float32.
+* A-terms: identity, or identity + ``aterm_sigma`` * complex N(0, 1), a new
+  draw every ``aterm_interval`` timesteps (one A-term slot per interval).
+* Taper: prolate spheroidal wave function psi_0(c, x) with c = 3 pi, separable
+  in x and y, peak 1.
+* Visibilities: real and imaginary parts N(0, 1) (generated on the device by
+  ``visibilities()`` for the large configurations).
+
+Plan: each baseline's time axis is cut into subgrids of
+``timesteps_per_subgrid`` consecutive integrations covering all channels; a
+subgrid's corner is placed so that its centre cell holds the centre of the
+uv extent of its visibilities (in wavelengths, over all its channels):
+``x = floor(u_mid * image_size + G/2 - S/2 + 1/2)``, the same for ``y``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import METADATA_DTYPE
+
+SPEED_OF_LIGHT = 299792458.0
+EARTH_ROTATION_RATE = 7.2921159e-5  # rad / s
+
+
+@dataclass
+class ObservationSpec:
+    nstations: int
+    disk_radius_m: float
+    ntimesteps: int            # integrations per baseline
+    timesteps_per_subgrid: int
+    nchannels: int
+    f_start: float
+    f_end: float
+    subgrid_size: int
+    grid_size: int
+    image_size: float
+    w_step: float = 0.0
+    integration_s: float = 1.0
+    dec_deg: float = -30.0
+    lat_deg: float = -30.0
+    aterm_sigma: float = 0.0   # 0 -> identity A-terms
+    aterm_interval: int = 0    # timesteps per A-term slot (0 -> one slot)
+    seed: int = 1234
+    taper_c: float = 3.0 * np.pi
+
+    @property
+    def n_baselines(self) -> int:
+        return self.nstations * (self.nstations - 1) // 2
+
+    @property
+    def subgrids_per_baseline(self) -> int:
+        return self.ntimesteps // self.timesteps_per_subgrid
+
+    @property
+    def n_subgrids(self) -> int:
+        return self.n_baselines * self.subgrids_per_baseline
+
+    @property
+    def n_rows(self) -> int:
+        return self.n_baselines * self.ntimesteps
+
+    @property
+    def n_aterm_slots(self) -> int:
+        if self.aterm_interval <= 0:
+            return 1
+        return (self.ntimesteps + self.aterm_interval - 1) // self.aterm_interval
+
+    @property
+    def n_visibilities(self) -> int:
+        return self.n_subgrids * self.timesteps_per_subgrid * self.nchannels
+
+
+# The BASELINE configurations of this benchmark (sizes as specified there).
+def config1(seed: int = 1) -> ObservationSpec:
+    """8 stations in a 3 km disk, 64 x 1 s, 16 ch 150-160 MHz, identity A-terms, S=32, G=512, 0.05 rad.
+
+    "An N km disk" is read as a disk N km across, so the longest baseline is N km."""
+    return ObservationSpec(nstations=8, disk_radius_m=1500.0, ntimesteps=64, timesteps_per_subgrid=64,
+                           nchannels=16, f_start=150e6, f_end=160e6, subgrid_size=32, grid_size=512,
+                           image_size=0.05, seed=seed)
+
+
+def config2(seed: int = 2) -> ObservationSpec:
+    """100 stations in a 10 km disk, 8192 x 1 s in 128-step subgrids, 16 ch, near-identity A-terms
+    renewed every 256 steps, S=32, G=4096, 0.05 rad: 4950 baselines, 316,800 subgrids, 6.49e8 visibilities."""
+    return ObservationSpec(nstations=100, disk_radius_m=5000.0, ntimesteps=8192, timesteps_per_subgrid=128,
+                           nchannels=16, f_start=150e6, f_end=160e6, subgrid_size=32, grid_size=4096,
+                           image_size=0.05, aterm_sigma=0.05, aterm_interval=256, seed=seed)
+
+
+@dataclass
+class Observation:
+    spec: ObservationSpec
+    stations: np.ndarray     # [ns, 3] ENU metres
+    baselines: np.ndarray    # [nb, 2] uint32
+    uvw: np.ndarray          # [nb*nt, 3] float32
+    frequencies: np.ndarray  # [C] float64
+    wavenumbers: np.ndarray  # [C] float32
+    aterms: np.ndarray       # [slots, ns, S, S, 4] complex64
+    taper: np.ndarray        # [S, S] float32
+    metadata: np.ndarray     # [N] METADATA_DTYPE
+
+
+def stations_in_disk(n: int, radius: float, rng: np.random.Generator) -> np.ndarray:
+    r = radius * np.sqrt(rng.random(n))
+    th = 2 * np.pi * rng.random(n)
+    return np.stack([r * np.cos(th), r * np.sin(th), np.zeros(n)], axis=1)
+
+
+def baseline_pairs(n: int) -> np.ndarray:
+    i, j = np.triu_indices(n, k=1)
+    return np.stack([i, j], axis=1).astype(np.uint32)
+
+
+def earth_rotation_uvw(enu: np.ndarray, hour_angles: np.ndarray, dec: float, lat: float) -> np.ndarray:
+    """uvw [nb, nt, 3] (float64) for baseline vectors enu [nb, 3]."""
+    E, N, U = enu[:, 0], enu[:, 1], enu[:, 2]
+    X = -np.sin(lat) * N + np.cos(lat) * U
+    Y = E
+    Z = np.cos(lat) * N + np.sin(lat) * U
+    sH, cH = np.sin(hour_angles)[None, :], np.cos(hour_angles)[None, :]
+    sd, cd = np.sin(dec), np.cos(dec)
+    X, Y, Z = X[:, None], Y[:, None], Z[:, None]
+    u = sH * X + cH * Y
+    v = -sd * cH * X + sd * sH * Y + cd * Z
+    w = cd * cH * X - cd * sH * Y + sd * Z
+    return np.stack([u, v, w], axis=-1)
+
+
+def pswf_taper(S: int, c: float = 3.0 * np.pi) -> np.ndarray:
+    """Separable prolate spheroidal taper psi_0(c, x) psi_0(c, y), peak 1."""
+    from scipy.special import pro_ang1
+
+    x = (np.arange(S) + 0.5 - S / 2) / (S / 2)
+    psi = np.array([pro_ang1(0, 0, c, xi)[0] for xi in x])
+    psi = psi / np.max(np.abs(psi))
+    return np.outer(psi, psi).astype(np.float32)
+
+
+def plan_subgrids(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.ndarray, baselines: np.ndarray) -> np.ndarray:
+    """uvw-driven plan (see the module docstring); returns METADATA_DTYPE[N]."""
+    nb, nt, T = spec.n_baselines, spec.ntimesteps, spec.timesteps_per_subgrid
+    nsub = spec.subgrids_per_baseline
+    S, G = spec.subgrid_size, spec.grid_size
+    u = uvw[:, 0].astype(np.float64).reshape(nb, nt)[:, : nsub * T].reshape(nb, nsub, T)
+    v = uvw[:, 1].astype(np.float64).reshape(nb, nt)[:, : nsub * T].reshape(nb, nsub, T)
+    f0, f1 = float(frequencies[0]), float(frequencies[-1])
+
+    def mid(a):
+        lo = np.minimum(a.min(axis=2) * f0, a.min(axis=2) * f1) / SPEED_OF_LIGHT
+        hi = np.maximum(a.max(axis=2) * f0, a.max(axis=2) * f1) / SPEED_OF_LIGHT
+        return 0.5 * (lo + hi)
+
+    x = np.floor(mid(u) * spec.image_size + G / 2 - S / 2 + 0.5).astype(np.int32)
+    y = np.floor(mid(v) * spec.image_size + G / 2 - S / 2 + 0.5).astype(np.int32)
+    md = np.zeros(nb * nsub, METADATA_DTYPE)
+    bl = np.repeat(np.arange(nb), nsub)
+    ts = np.tile(np.arange(nsub), nb)
+    md["baseline_offset"] = 0
+    md["time_offset"] = bl * nt + ts * T
+    md["nr_timesteps"] = T
+    md["aterm_index"] = (ts * T) // spec.aterm_interval if spec.aterm_interval > 0 else 0
+    md["station1"] = baselines[bl, 0]
+    md["station2"] = baselines[bl, 1]
+    md["x"] = x.reshape(-1)
+    md["y"] = y.reshape(-1)
+    md["z"] = 0
+    return md
+
+
+def uv_extent_pixels(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.ndarray) -> np.ndarray:
+    """Per subgrid, the larger of its u and v extents in grid cells (must stay below S minus the taper support)."""
+    nb, nt, T = spec.n_baselines, spec.ntimesteps, spec.timesteps_per_subgrid
+    nsub = spec.subgrids_per_baseline
+    f0, f1 = float(frequencies[0]), float(frequencies[-1])
+    ext = []
+    for k in (0, 1):
+        a = uvw[:, k].astype(np.float64).reshape(nb, nt)[:, : nsub * T].reshape(nb, nsub, T)
+        lo = np.minimum(a.min(axis=2) * f0, a.min(axis=2) * f1)
+        hi = np.maximum(a.max(axis=2) * f0, a.max(axis=2) * f1)
+        ext.append((hi - lo) / SPEED_OF_LIGHT * spec.image_size)
+    return np.maximum(ext[0], ext[1]).reshape(-1)
+
+
+def make_observation(spec: ObservationSpec) -> Observation:
+    rng = np.random.default_rng(spec.seed)
+    st = stations_in_disk(spec.nstations, spec.disk_radius_m, rng)
+    bl = baseline_pairs(spec.nstations)
+    enu = st[bl[:, 1]] - st[bl[:, 0]]
+    H = (np.arange(spec.ntimesteps) - (spec.ntimesteps - 1) / 2.0) * spec.integration_s * EARTH_ROTATION_RATE
+    uvw = earth_rotation_uvw(enu, H, np.deg2rad(spec.dec_deg), np.deg2rad(spec.lat_deg))
+    uvw = uvw.reshape(-1, 3).astype(np.float32)
+    freqs = np.linspace(spec.f_start, spec.f_end, spec.nchannels) if spec.nchannels > 1 else np.array([spec.f_start])
+    k = (2 * np.pi * freqs / SPEED_OF_LIGHT).astype(np.float32)
+    S = spec.subgrid_size
+    at = np.zeros((spec.n_aterm_slots, spec.nstations, S, S, 4), np.complex64)
+    at[..., 0] = 1
+    at[..., 3] = 1
+    if spec.aterm_sigma > 0:
+        noise = rng.standard_normal((*at.shape, 2), dtype=np.float32)
+        at += (spec.aterm_sigma * (noise[..., 0] + 1j * noise[..., 1])).astype(np.complex64)
+    taper = pswf_taper(S, spec.taper_c)
+    md = plan_subgrids(spec, uvw, freqs, bl)
+    return Observation(spec, st, bl, uvw, freqs, k, at, taper, md)
+
+
+def visibilities(spec: ObservationSpec, device="cpu", seed: int | None = None):
+    """[rows, C, 4] complex64 with N(0,1) real and imaginary parts (torch tensor on `device`)."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(spec.seed if seed is None else seed)
+    n = spec.n_rows * spec.nchannels * 4
+    re_im = torch.randn(n * 2, generator=g, device=device, dtype=torch.float32)
+    return torch.view_as_complex(re_im.view(-1, 2)).view(spec.n_rows, spec.nchannels, 4)

@@ -1,0 +1,210 @@
+"""Device-level IDG operations on CUDA tensors, through the C ABI.
+
+Each function validates shapes and dtypes on the host and calls the matching
+``idg_*`` entry point on the tensor's device and the current (or given)
+stream.  Layouts are those of include/idg_gb300.h.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import IdgParams, ptr
+
+VARIANT_PLAIN = _lib.VARIANT_PLAIN
+VARIANT_BATCHED = _lib.VARIANT_BATCHED
+
+
+@dataclass
+class GridSpec:
+    """Geometry and physics of one gridding problem (idg_params)."""
+
+    grid_size: int
+    subgrid_size: int
+    nr_channels: int
+    nr_stations: int
+    nr_aterms: int = 1
+    nr_w_planes: int = 1
+    image_size: float = 0.1
+    w_step: float = 0.0
+    flags: int = 0
+
+    def to_c(self) -> IdgParams:
+        return IdgParams(self.grid_size, self.subgrid_size, self.nr_channels, self.nr_stations, self.nr_aterms,
+                         self.nr_w_planes, self.image_size, self.w_step, self.flags, 0)
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _req(t: torch.Tensor, name: str, dtype, shape=None):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch.Tensor")
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+
+
+def metadata_tensor(md: np.ndarray, device) -> torch.Tensor:
+    """Plan entries (METADATA_DTYPE) as an int32 [N, 9] device tensor."""
+    md = np.ascontiguousarray(md, dtype=_lib.METADATA_DTYPE)
+    return torch.from_numpy(md.view(np.int32).reshape(-1, 9).copy()).to(device)
+
+
+def ext_tensor(ext: np.ndarray | None, device) -> torch.Tensor | None:
+    if ext is None:
+        return None
+    ext = np.ascontiguousarray(ext, dtype=_lib.SUBGRID_EXT_DTYPE)
+    return torch.from_numpy(ext.view(np.int32).reshape(-1, 2).copy()).to(device)
+
+
+def _check_common(spec: GridSpec, metadata, uvw, wavenumbers, vis, taper, aterms):
+    _req(metadata, "metadata", torch.int32)
+    if metadata.dim() != 2 or metadata.shape[1] != 9:
+        raise ValueError("metadata must be [N, 9] int32 (36-byte entries)")
+    _req(uvw, "uvw", torch.float32)
+    if uvw.dim() != 2 or uvw.shape[1] != 3:
+        raise ValueError("uvw must be [rows, 3] float32")
+    _req(wavenumbers, "wavenumbers", torch.float32, (spec.nr_channels,))
+    _req(vis, "visibilities", torch.complex64, (uvw.shape[0], spec.nr_channels, 4))
+    S = spec.subgrid_size
+    if taper is not None:
+        _req(taper, "spheroidal", torch.float32, (S, S))
+    _req(aterms, "aterms", torch.complex64, (spec.nr_aterms, spec.nr_stations, S, S, 4))
+
+
+def gridder(spec: GridSpec, metadata, uvw, wavenumbers, vis, taper, aterms, subgrids, variant=VARIANT_PLAIN,
+            ext=None, stream=None):
+    """subgrids[N,4,S,S] complex64 <- gridder(vis)."""
+    _check_common(spec, metadata, uvw, wavenumbers, vis, taper, aterms)
+    N, S = metadata.shape[0], spec.subgrid_size
+    _req(subgrids, "subgrids", torch.complex64, (N, 4, S, S))
+    if ext is not None:
+        _req(ext, "ext", torch.int32, (N, 2))
+    p = spec.to_c()
+    _lib.call("idg_gridder", ctypes.byref(p), variant, N, ptr(metadata), ptr(ext), uvw.shape[0], ptr(uvw),
+              ptr(wavenumbers), ptr(vis), ptr(taper), ptr(aterms), ptr(subgrids), _stream_handle(stream))
+    return subgrids
+
+
+def degridder(spec: GridSpec, metadata, uvw, wavenumbers, vis, taper, aterms, subgrids, variant=VARIANT_PLAIN,
+              ext=None, stream=None):
+    """vis[rows named by the plan] <- degridder(subgrids)."""
+    _check_common(spec, metadata, uvw, wavenumbers, vis, taper, aterms)
+    N, S = metadata.shape[0], spec.subgrid_size
+    _req(subgrids, "subgrids", torch.complex64, (N, 4, S, S))
+    if ext is not None:
+        _req(ext, "ext", torch.int32, (N, 2))
+    p = spec.to_c()
+    _lib.call("idg_degridder", ctypes.byref(p), variant, N, ptr(metadata), ptr(ext), uvw.shape[0], ptr(uvw),
+              ptr(wavenumbers), ptr(vis), ptr(taper), ptr(aterms), ptr(subgrids), _stream_handle(stream))
+    return vis
+
+
+def subgrid_fft(spec: GridSpec, subgrids, direction: int, taper=None, stream=None):
+    """In-place FFT of subgrids[N,4,S,S]; direction +1 image->uv, -1 uv->image."""
+    S = spec.subgrid_size
+    _req(subgrids, "subgrids", torch.complex64)
+    if subgrids.dim() != 4 or subgrids.shape[1:] != (4, S, S):
+        raise ValueError("subgrids must be [N, 4, S, S]")
+    if taper is not None:
+        _req(taper, "taper", torch.float32, (S, S))
+    p = spec.to_c()
+    _lib.call("idg_subgrid_fft", ctypes.byref(p), subgrids.shape[0], int(direction), ptr(taper), ptr(subgrids),
+              _stream_handle(stream))
+    return subgrids
+
+
+def adder(spec: GridSpec, metadata, subgrids, grid, stream=None):
+    S, G, W = spec.subgrid_size, spec.grid_size, spec.nr_w_planes
+    _req(metadata, "metadata", torch.int32)
+    _req(subgrids, "subgrids", torch.complex64, (metadata.shape[0], 4, S, S))
+    _req(grid, "grid", torch.complex64, (W, 4, G, G))
+    p = spec.to_c()
+    _lib.call("idg_adder", ctypes.byref(p), metadata.shape[0], ptr(metadata), ptr(subgrids), ptr(grid),
+              _stream_handle(stream))
+    return grid
+
+
+def splitter(spec: GridSpec, metadata, grid, subgrids, stream=None):
+    S, G, W = spec.subgrid_size, spec.grid_size, spec.nr_w_planes
+    _req(metadata, "metadata", torch.int32)
+    _req(subgrids, "subgrids", torch.complex64, (metadata.shape[0], 4, S, S))
+    _req(grid, "grid", torch.complex64, (W, 4, G, G))
+    p = spec.to_c()
+    _lib.call("idg_splitter", ctypes.byref(p), metadata.shape[0], ptr(metadata), ptr(grid), ptr(subgrids),
+              _stream_handle(stream))
+    return subgrids
+
+
+def grid_visibilities(spec: GridSpec, metadata, uvw, wavenumbers, vis, taper, aterms, subgrids, grid,
+                      variant=VARIANT_BATCHED, ext=None, stream=None):
+    """Gridding step: gridder -> subgrid FFT (+1, taper) -> adder; accumulates into grid[W,4,G,G]."""
+    _check_common(spec, metadata, uvw, wavenumbers, vis, taper, aterms)
+    N, S, G, W = metadata.shape[0], spec.subgrid_size, spec.grid_size, spec.nr_w_planes
+    _req(subgrids, "subgrids", torch.complex64, (N, 4, S, S))
+    _req(grid, "grid", torch.complex64, (W, 4, G, G))
+    p = spec.to_c()
+    _lib.call("idg_grid_visibilities", ctypes.byref(p), variant, N, ptr(metadata), ptr(ext), uvw.shape[0], ptr(uvw),
+              ptr(wavenumbers), ptr(vis), ptr(taper), ptr(aterms), ptr(subgrids), ptr(grid), _stream_handle(stream))
+    return grid
+
+
+def degrid_visibilities(spec: GridSpec, metadata, uvw, wavenumbers, vis, taper, aterms, subgrids, grid,
+                        variant=VARIANT_BATCHED, ext=None, stream=None):
+    """Degridding step: splitter -> subgrid FFT (-1, taper) -> degridder into vis."""
+    _check_common(spec, metadata, uvw, wavenumbers, vis, taper, aterms)
+    N, S, G, W = metadata.shape[0], spec.subgrid_size, spec.grid_size, spec.nr_w_planes
+    _req(subgrids, "subgrids", torch.complex64, (N, 4, S, S))
+    _req(grid, "grid", torch.complex64, (W, 4, G, G))
+    p = spec.to_c()
+    _lib.call("idg_degrid_visibilities", ctypes.byref(p), variant, N, ptr(metadata), ptr(ext), uvw.shape[0],
+              ptr(uvw), ptr(wavenumbers), ptr(vis), ptr(taper), ptr(aterms), ptr(subgrids), ptr(grid),
+              _stream_handle(stream))
+    return vis
+
+
+def imaging_cycle(spec: GridSpec, metadata: np.ndarray, uvw: np.ndarray, wavenumbers: np.ndarray, vis_in, taper,
+                  aterms, vis_out, grid_out=None, variant=VARIANT_BATCHED, chunk_subgrids=0) -> dict:
+    """One grid + degrid cycle on HOST buffers (numpy arrays or pinned CPU tensors) through idg_imaging_cycle."""
+    md = np.ascontiguousarray(metadata, dtype=_lib.METADATA_DTYPE)
+    for name, a in (("uvw", uvw), ("wavenumbers", wavenumbers), ("taper", taper)):
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]):
+            raise TypeError(f"{name} must be a C-contiguous float32 numpy array")
+    t = _lib.IdgCycleTiming()
+    p = spec.to_c()
+    _lib.call("idg_imaging_cycle", ctypes.byref(p), variant, md.shape[0], ptr(md), uvw.shape[0], ptr(uvw),
+              ptr(wavenumbers), ptr(vis_in), ptr(taper), ptr(aterms), ptr(vis_out), ptr(grid_out),
+              int(chunk_subgrids), ctypes.byref(t))
+    return {"total_ms": t.total_ms, "gridding_ms": t.gridding_ms, "degridding_ms": t.degridding_ms,
+            "h2d_bytes": t.h2d_bytes, "d2h_bytes": t.d2h_bytes, "kernel_launches": t.kernel_launches}
+
+
+def release_buffers() -> None:
+    _lib.call("idg_release_buffers")
+
+
+def device_status(clear: bool = True, stream=None) -> int:
+    v = ctypes.c_uint32(0)
+    _lib.call("idg_device_status", _stream_handle(stream), ctypes.byref(v), 1 if clear else 0)
+    return int(v.value)
+
+
+def measure_fp32_peak() -> float:
+    f = ctypes.c_double(0)
+    _lib.call("idg_measure_fp32_peak", ctypes.byref(f))
+    return float(f.value)

@@ -1,0 +1,181 @@
+"""Parity of the CUDA kernels (through the C ABI) with the FP64 oracle.
+
+Tolerance: relative RMS error <= 1e-5 against the FP64 oracle evaluated on
+the same float inputs, for gridder and degridder outputs (the benchmark's
+accuracy target); the subgrid FFT, adder and splitter are FP32 transforms of
+FP32 data and are held to 2e-6.
+"""
+import numpy as np
+import pytest
+import torch
+
+import idg_gb300._lib as L
+from conftest import golden_cases, load_golden, rel_rms
+from gpu_helpers import degrid_gpu, dev, grid_gpu, spec_for
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+VARIANTS = [L.VARIANT_PLAIN, L.VARIANT_BATCHED]
+
+
+def _config1_obs(**over):
+    from idg_gb300 import datasets as D
+
+    spec = D.config1()
+    for k, v in over.items():
+        setattr(spec, k, v)
+    return spec, D.make_observation(spec)
+
+
+def _vis(spec, seed=7):
+    rng = np.random.default_rng(seed)
+    return (rng.standard_normal((spec.n_rows, spec.nchannels, 4)) +
+            1j * rng.standard_normal((spec.n_rows, spec.nchannels, 4))).astype(np.complex64)
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_gridder_config1_vs_fp64(oracle_mod, idg, variant):
+    spec, obs = _config1_obs()
+    vis = _vis(spec)
+    sp = spec_for(spec.grid_size, spec.subgrid_size, spec.nchannels, spec.nstations, obs.aterms.shape[0],
+                  spec.image_size)
+    got = grid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, variant)
+    prm = oracle_mod.params(spec.grid_size, spec.subgrid_size, spec.nchannels, spec.nstations, spec.n_subgrids,
+                            spec.image_size)
+    want = oracle_mod.gridder(prm, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, obs.metadata)
+    assert rel_rms(got, want) <= TOL
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("refcpu", [False, True])
+def test_degridder_config1_vs_fp64(oracle_mod, idg, variant, refcpu):
+    spec, obs = _config1_obs(aterm_sigma=0.05)
+    rng = np.random.default_rng(11)
+    S = spec.subgrid_size
+    sub = (rng.standard_normal((spec.n_subgrids, 4, S, S)) + 1j * rng.standard_normal((spec.n_subgrids, 4, S, S))).astype(np.complex64)
+    flags = L.IDG_FLAG_DEGRID_ATERM_REFCPU if refcpu else 0
+    sp = spec_for(spec.grid_size, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size, flags=flags)
+    got = degrid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, spec.n_rows, variant)
+    prm = oracle_mod.params(spec.grid_size, S, spec.nchannels, spec.nstations, spec.n_subgrids, spec.image_size)
+    want = oracle_mod.degridder(prm, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, obs.metadata, spec.n_rows,
+                                aterm_mode=oracle_mod.ATERM_REFCPU if refcpu else oracle_mod.ATERM_ADJOINT)
+    assert rel_rms(got, want) <= TOL
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: p.rsplit("/", 1)[-1])
+def test_reference_inputs_gridder_and_degridder(oracle_mod, idg, path):
+    """The reference's own inputs and random plan (image_size 0.1): FP64 oracle within 1e-5,
+    and the reference's FP32 CPU output within its own FP32 error (5e-4)."""
+    d = load_golden(path)
+    G, S, ns, C, nts, T = d["cfg"]
+    nsg = d["metadata"].shape[0]
+    sp = spec_for(G, S, C, ns, nts, 0.1, flags=L.IDG_FLAG_DEGRID_ATERM_REFCPU)
+    prm = oracle_mod.params(G, S, C, ns, nsg, 0.1)
+    for variant in VARIANTS:
+        got = grid_gpu(sp, d["metadata"], d["uvw"], d["wavenumbers"], d["vis"], d["spheroidal"], d["aterms"], variant)
+        want = oracle_mod.gridder(prm, d["uvw"], d["wavenumbers"], d["vis"], d["spheroidal"], d["aterms"], d["metadata"])
+        assert rel_rms(got, want) <= TOL
+        assert rel_rms(d["gridder_out"], got) < 5e-4
+        vg = degrid_gpu(sp, d["metadata"], d["uvw"], d["wavenumbers"], d["degridder_in"], d["spheroidal"],
+                        d["aterms"], d["vis"].shape[0], variant)
+        vw = oracle_mod.degridder(prm, d["uvw"], d["wavenumbers"], d["degridder_in"], d["spheroidal"], d["aterms"],
+                                  d["metadata"], d["vis"].shape[0], aterm_mode=oracle_mod.ATERM_REFCPU)
+        assert rel_rms(vg, vw) <= TOL
+        assert rel_rms(d["degridder_out"], vg) < 5e-4
+
+
+def test_config2_sample_vs_fp64(oracle_mod, idg):
+    """48 subgrids of the full config-2 plan (including the longest baselines)."""
+    from idg_gb300 import datasets as D
+
+    spec = D.config2()
+    obs = D.make_observation(spec)
+    bl_len = np.linalg.norm(obs.uvw[:: spec.ntimesteps, :2], axis=1)
+    order = np.argsort(bl_len)
+    pick_bl = np.concatenate([order[:8], order[len(order) // 2: len(order) // 2 + 8], order[-8:]])
+    subs = np.concatenate([b * spec.subgrids_per_baseline + np.array([0, spec.subgrids_per_baseline - 1]) for b in pick_bl])
+    md = obs.metadata[subs].copy()
+    # compact the rows these subgrids use
+    rows = np.concatenate([np.arange(m["time_offset"], m["time_offset"] + m["nr_timesteps"]) for m in md])
+    uvw = obs.uvw[rows]
+    md["time_offset"] = np.arange(len(md)) * spec.timesteps_per_subgrid
+    rng = np.random.default_rng(5)
+    vis = (rng.standard_normal((len(rows), spec.nchannels, 4)) + 1j * rng.standard_normal((len(rows), spec.nchannels, 4))).astype(np.complex64)
+    S = spec.subgrid_size
+    sp = spec_for(spec.grid_size, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    prm = oracle_mod.params(spec.grid_size, S, spec.nchannels, spec.nstations, len(md), spec.image_size)
+    want = oracle_mod.gridder(prm, uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, md)
+    for variant in VARIANTS:
+        got = grid_gpu(sp, md, uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, variant)
+        assert rel_rms(got, want) <= TOL
+    sub = (rng.standard_normal((len(md), 4, S, S)) + 1j * rng.standard_normal((len(md), 4, S, S))).astype(np.complex64)
+    vwant = oracle_mod.degridder(prm, uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, md, len(rows))
+    for variant in VARIANTS:
+        vgot = degrid_gpu(sp, md, uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, len(rows), variant)
+        assert rel_rms(vgot, vwant) <= TOL
+
+
+@pytest.mark.parametrize("S", [8, 16, 24, 32, 48, 64])
+def test_subgrid_fft_vs_dft(oracle_mod, idg, S):
+    from idg_gb300 import ops
+
+    rng = np.random.default_rng(S)
+    N = 5
+    P = (rng.standard_normal((N, 4, S, S)) + 1j * rng.standard_normal((N, 4, S, S))).astype(np.complex64)
+    taper = rng.random((S, S)).astype(np.float32)
+    sp = spec_for(1024, S, 1, 2, 1, 0.05)
+    for direction in (1, -1):
+        for tp in (None, taper):
+            x = dev(P)
+            ops.subgrid_fft(sp, x, direction, dev(tp) if tp is not None else None)
+            torch.cuda.synchronize()
+            want = oracle_mod.subgrid_dft(P, direction, tp)
+            assert rel_rms(x.cpu().numpy(), want) <= 2e-6, (direction, tp is not None)
+    x = dev(P)
+    ops.subgrid_fft(sp, x, 1)
+    ops.subgrid_fft(sp, x, -1)
+    torch.cuda.synchronize()
+    assert rel_rms(x.cpu().numpy() / (S * S), P) <= 2e-6
+
+
+def test_adder_splitter_vs_oracle(oracle_mod, idg):
+    from idg_gb300 import ops
+
+    S, G, W = 16, 96, 2
+    rng = np.random.default_rng(2)
+    N = 40
+    md = np.zeros(N, L.METADATA_DTYPE)
+    md["x"] = rng.integers(-S + 2, G - 2, N)
+    md["y"] = rng.integers(-S + 2, G - 2, N)
+    md["z"] = rng.integers(0, W, N)
+    md["z"][0] = 5  # outside the w-planes: skipped by the adder, zeros from the splitter
+    sub = (rng.standard_normal((N, 4, S, S)) + 1j * rng.standard_normal((N, 4, S, S))).astype(np.complex64)
+    sp = spec_for(G, S, 1, 2, 1, 0.05, W=W)
+    grid = torch.zeros((W, 4, G, G), dtype=torch.complex64, device="cuda")
+    ops.adder(sp, dev(md), dev(sub), grid)
+    torch.cuda.synchronize()
+    want = oracle_mod.adder(sub, md, G, W)
+    assert rel_rms(grid.cpu().numpy(), want) <= 2e-6
+    g = (rng.standard_normal((W, 4, G, G)) + 1j * rng.standard_normal((W, 4, G, G))).astype(np.complex64)
+    out = torch.empty((N, 4, S, S), dtype=torch.complex64, device="cuda")
+    ops.splitter(sp, dev(md), dev(g), out)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), oracle_mod.splitter(g, md, S).astype(np.complex64))
+
+
+def test_bad_plan_entry_is_flagged_not_faulted(idg):
+    from idg_gb300 import ops
+
+    spec, obs = _config1_obs()
+    vis = _vis(spec)
+    md = obs.metadata.copy()
+    md["time_offset"][3] = spec.n_rows  # rows past the end
+    md["station2"][5] = 999             # station out of range
+    sp = spec_for(spec.grid_size, spec.subgrid_size, spec.nchannels, spec.nstations, 1, spec.image_size)
+    ops.device_status(clear=True)
+    got = grid_gpu(sp, md, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms)
+    assert ops.device_status(clear=True) & 1
+    assert np.all(got[3] == 0) and np.all(got[5] == 0)
+    assert np.any(got[4] != 0)
+    assert ops.device_status(clear=True) == 0

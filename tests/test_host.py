@@ -1,0 +1,132 @@
+"""Host logic: YAML configuration, result table / CSV format, synthetic
+observations and the uvw-driven plan.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def test_yaml_subset_parses_reference_examples(idg, tmp_path):
+    from idg_gb300 import config as C
+
+    text = """grid_size: 1024
+operation_types: [gridding, degridding]
+niterations: 100
+nstations: 2
+ntimeslots: 2
+ntimesteps_per_subgrid: 128
+nchannels: 16
+subgrid_size: 32
+hardware_types: [gpu]
+"""
+    p = tmp_path / "example.yaml"
+    p.write_text(text)
+    cfgs = C.read_configuration(str(p))
+    assert [c.operation.value for c in cfgs] == ["gridding", "degridding"]
+    c = cfgs[0]
+    assert (c.grid_size, c.niterations, c.nstations, c.ntimeslots, c.ntimesteps_per_subgrid, c.nchannels,
+            c.subgrid_size) == (1024, 100, 2, 2, 128, 16, 32)
+    assert c.image_size == pytest.approx(0.1) and c.w_step == 0.0
+
+
+def test_yaml_block_lists_and_comments(idg, tmp_path):
+    from idg_gb300 import config as C
+
+    y = C.parse_yaml_subset("a: 3  # comment\nhardware_types:\n  - gpu\n  - gpu\nb: [x, 'y']\n")
+    assert y == {"a": 3, "hardware_types": ["gpu", "gpu"], "b": ["x", "y"]}
+
+
+@pytest.mark.parametrize(
+    "body, message",
+    [
+        ("operation_types: [gridding]\n", "hardware_types section empty."),
+        ("hardware_types: [tpu]\noperation_types: [gridding]\n", "Invalid hardware_type token tpu"),
+        ("hardware_types: [cpu]\noperation_types: [gridding]\n", "CPU support is disabled"),
+        ("hardware_types: [gpu]\n", "operation_types section empty."),
+        ("hardware_types: [gpu]\noperation_types: [fft]\n", "Invalid operation type token fft"),
+        ("hardware_types: [gpu]\noperation_types: [gridding]\n", "Invalid grid_size section"),
+    ],
+)
+def test_config_errors(idg, tmp_path, body, message):
+    from idg_gb300 import config as C
+
+    p = tmp_path / "bad.yaml"
+    p.write_text(body)
+    with pytest.raises(C.ConfigError) as e:
+        C.read_configuration(str(p))
+    assert message in str(e.value)
+
+
+def test_missing_file(idg):
+    from idg_gb300 import config as C
+
+    with pytest.raises(C.ConfigError, match="not found"):
+        C.read_configuration("/nonexistent/x.yaml")
+
+
+def test_csv_and_table_format(idg, tmp_path, monkeypatch):
+    from idg_gb300 import config as C
+    from idg_gb300 import launcher as L
+
+    cfg = L.configuration(niterations=3)
+    r = L.benchmark_result(in_transfer_time=12.5, compute_time=100.0)
+    rows = C.result_rows([cfg], [r])
+    assert rows[0] == C.RESULT_LABELS and len(rows[0]) == 12
+    assert rows[1][:3] == ["0", "gridding", "3"]
+    assert rows[1][7] == "12.500000" and rows[1][8] == "N/A" and rows[1][9] == "100.000000"
+    monkeypatch.chdir(tmp_path)
+    written = C.write_csv(os.path.join("some", "dir", "out.csv"), rows)
+    assert written == "out.csv"
+    lines = (tmp_path / "out.csv").read_text().split("\n")
+    assert lines[0].endswith(";") and lines[0].count(";") == 12
+    assert lines[1].startswith("0;gridding;3;")
+    assert lines[-1] == ""
+
+
+def test_observation_geometry_and_plan(idg):
+    from idg_gb300 import datasets as D
+
+    spec = D.config1()
+    obs = D.make_observation(spec)
+    assert obs.uvw.shape == (spec.n_rows, 3) and obs.uvw.dtype == np.float32
+    assert spec.n_baselines == 28 and spec.n_subgrids == 28 and spec.n_visibilities == 28672
+    # baseline lengths within the disk diameter; w non-zero (earth rotation at dec -30)
+    assert np.linalg.norm(obs.uvw, axis=1).max() <= 2 * spec.disk_radius_m + 1e-3
+    assert np.abs(obs.uvw[:, 2]).max() > 1.0
+    # plan: every subgrid inside the grid and its uv extent fits with room for the taper
+    md = obs.metadata
+    S, G = spec.subgrid_size, spec.grid_size
+    assert (md["x"] >= 0).all() and (md["x"] + S <= G).all() and (md["y"] >= 0).all() and (md["y"] + S <= G).all()
+    assert D.uv_extent_pixels(spec, obs.uvw, obs.frequencies).max() < S - 8
+    # the subgrid centre sits on the visibilities' uv centre (within half a cell)
+    u = obs.uvw[:, 0].reshape(spec.n_baselines, -1).astype(np.float64)
+    f = obs.frequencies
+    u_lam = np.concatenate([u * f[0], u * f[-1]], axis=1) / D.SPEED_OF_LIGHT
+    mid = 0.5 * (u_lam.min(1) + u_lam.max(1))
+    centre = (md["x"] + S / 2 - G / 2) / spec.image_size
+    assert np.all(np.abs(centre - mid) <= 0.5 / spec.image_size + 1e-6)
+    # taper: separable, peak 1, small at the edges
+    t = obs.taper
+    assert t.shape == (S, S) and abs(t.max() - 1) < 1e-6 and t[0, 0] < 1e-3
+    assert np.allclose(t, np.outer(t[S // 2], t[S // 2]) / t[S // 2, S // 2], atol=1e-6)
+
+
+def test_config2_sizes(idg):
+    from idg_gb300 import datasets as D
+
+    spec = D.config2()
+    assert spec.n_baselines == 4950
+    assert spec.n_subgrids == 316800
+    assert spec.n_visibilities == 648806400
+    assert spec.n_aterm_slots == 32
+
+
+def test_plan_is_deterministic(idg):
+    from idg_gb300 import datasets as D
+
+    a = D.make_observation(D.config1())
+    b = D.make_observation(D.config1())
+    assert np.array_equal(a.metadata.view(np.uint8), b.metadata.view(np.uint8))
+    assert np.array_equal(a.uvw, b.uvw)
