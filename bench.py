@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of each baseline half")
+    ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline (profiling runs)")
+    ap.add_argument("--max-subgrids", type=int, default=0, help="use only the first N subgrids of the plan (profiling)")
     return ap.parse_args()
 
 
@@ -197,6 +199,9 @@ def run_ours(args, rank, world, local_rank):
 
     spec = workload_spec(args.workload, seed=2 if args.workload == "config2" else 1)
     obs = D.make_observation(spec)
+    if args.max_subgrids:
+        obs = D.truncate_observation(obs, args.max_subgrids)
+        spec = obs.spec
     S, C, G = spec.subgrid_size, spec.nchannels, spec.grid_size
     N = spec.n_subgrids
     gs = ops.GridSpec(G, S, C, spec.nstations, obs.aterms.shape[0], 1, spec.image_size, spec.w_step)
@@ -339,7 +344,7 @@ def run_ours(args, rank, world, local_rank):
         ops.release_buffers()
         del out_host
 
-    if rank == 0:
+    if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(obs, vis_host.numpy() if vis_host is not None else None, args.cpu_seconds)
 
     if dist:

@@ -165,27 +165,6 @@ __global__ void __launch_bounds__(kThreads) degridder_plain_kernel(KernelArgs a)
     degrid_subgrid(a, si, s, sm->pix, sm->geo, sm->coef, kappa_s);
 }
 
-__global__ void __launch_bounds__(kThreads) degridder_persistent_kernel(KernelArgs a) {
-    extern __shared__ float4 smem[];
-    __shared__ int next;
-    DegridSmem *sm = reinterpret_cast<DegridSmem *>(smem);
-    float *kappa_s = reinterpret_cast<float *>(sm + 1);
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) next = atomicAdd(a.work_counter, 1);
-        __syncthreads();
-        const int idx = next;
-        if (idx >= a.nr_subgrids) break;
-        const int s = a.work_list ? a.work_list[idx] : idx;
-        const SubgridInfo si = load_subgrid(a, s);
-        if (!si.ok) {
-            if (threadIdx.x == 0) flag_status(a.status, kStatusBadPlan);
-            continue;
-        }
-        degrid_subgrid(a, si, s, sm->pix, sm->geo, sm->coef, kappa_s);
-    }
-}
-
 } // namespace
 
 cudaError_t launch_degridder(const KernelArgs &a, int variant, int max_nc, cudaStream_t stream) {
@@ -197,19 +176,7 @@ cudaError_t launch_degridder(const KernelArgs &a, int variant, int max_nc, cudaS
         degridder_plain_kernel<<<(unsigned)a.nr_subgrids, kThreads, smem, stream>>>(a);
         return cudaGetLastError();
     }
-    cudaError_t e =
-        cudaFuncSetAttribute(degridder_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degridder_persistent_kernel, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
-    if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
-    degridder_persistent_kernel<<<(unsigned)blocks, kThreads, smem, stream>>>(a);
-    return cudaGetLastError();
+    return launch_degridder_fast(a, stream);
 }
 
 } // namespace idg

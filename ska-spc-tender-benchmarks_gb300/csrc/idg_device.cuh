@@ -28,7 +28,7 @@ constexpr float kTwoPiF = 6.28318530717958647692f;
 constexpr double kTwoPi = 6.28318530717958647692;
 
 // Device-side check word (see idg_device_status()), one per device.
-enum : unsigned { kStatusBadPlan = 1u, kStatusBadShape = 2u };
+enum : unsigned { kStatusBadPlan = 1u, kStatusBadShape = 2u, kStatusTimeout = 4u };
 
 __device__ __forceinline__ void flag_status(unsigned *status, unsigned bits) {
     if (status) atomicOr(status, bits);

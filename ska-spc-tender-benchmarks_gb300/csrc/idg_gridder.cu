@@ -149,32 +149,6 @@ __global__ void __launch_bounds__(kThreads) gridder_plain_kernel(KernelArgs a) {
     grid_subgrid(a, si, s, coef_s, vis_s, kappa_s);
 }
 
-// Persistent variant: CTAs pull subgrids from a work list (cost-sorted on the
-// host) through a global counter, so subgrids with uneven visibility counts
-// balance across the SMs in one launch.
-__global__ void __launch_bounds__(kThreads) gridder_persistent_kernel(KernelArgs a, int max_nc) {
-    extern __shared__ float4 smem[];
-    __shared__ int next;
-    float4 *coef_s = smem;
-    float4 *vis_s = coef_s + kCoefSlots;
-    float *kappa_s = (float *)(vis_s + kVisSlots);
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) next = atomicAdd(a.work_counter, 1);
-        __syncthreads();
-        const int idx = next;
-        if (idx >= a.nr_subgrids) break;
-        const int s = a.work_list ? a.work_list[idx] : idx;
-        const SubgridInfo si = load_subgrid(a, s);
-        if (!si.ok || si.c1 - si.c0 > max_nc) {
-            if (threadIdx.x == 0) flag_status(a.status, si.ok ? kStatusBadShape : kStatusBadPlan);
-            zero_subgrid(a, s);
-            continue;
-        }
-        grid_subgrid(a, si, s, coef_s, vis_s, kappa_s);
-    }
-}
-
 size_t smem_bytes_for(int max_nc) { return (size_t)(kCoefSlots + kVisSlots) * 16 + (size_t)max_nc * 4 + 16; }
 
 } // namespace
@@ -187,18 +161,7 @@ cudaError_t launch_gridder(const KernelArgs &a, int variant, int max_nc, cudaStr
         gridder_plain_kernel<<<(unsigned)a.nr_subgrids, kThreads, smem, stream>>>(a);
         return cudaGetLastError();
     }
-    cudaError_t e = cudaFuncSetAttribute(gridder_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gridder_persistent_kernel, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
-    if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
-    gridder_persistent_kernel<<<(unsigned)blocks, kThreads, smem, stream>>>(a, max_nc);
-    return cudaGetLastError();
+    return launch_gridder_fast(a, stream);
 }
 
 } // namespace idg

@@ -1,0 +1,341 @@
+// idg_gridder_fast.cu -- the batched gridder: persistent CTAs, TMA-staged
+// visibilities, packed-FP32 pixel pairs.
+//
+// Same result as the plain gridder (idg_gridder.cu): subgrid = taper * A1^H P A2
+// with P = sum_{t,c} V[t][c] exp(i phase), phase carried with FP64 per-subgrid
+// offsets.  Differences in how the work is done:
+//  * CTAs are persistent and pull subgrids from a global counter (optionally
+//    through a cost-sorted work list), so uneven subgrids balance in one launch.
+//  * Each thread owns 4 pixel PAIRS (8 pixels, two adjacent x per pair) and
+//    keeps their accumulators as packed FP32x2 registers: every complex MAC of
+//    a pixel pair is two fma.rn.f32x2, halving issue slots per pixel-visibility
+//    (17 FMA of work issue as ~9 instructions).
+//  * A tile of visibilities is copied global -> shared with cp.async.bulk (one
+//    bulk copy per row, completion counted on an mbarrier, bounded wait) and
+//    expanded once per tile into the operand pairs the packed MACs read as
+//    warp-wide broadcasts: (re,re), (im,im), (-im,-im) per correlation.
+//  * The phase is kept in radians: per (pixel pair, timestep) the FP64-derived
+//    offset part tau0 is reduced to [-pi, pi]; per channel x = tau0 + kappa*Q.
+//    When a tile's bound pi + max|kappa| max|Q| stays below kFastBound the
+//    sincos takes x directly (the SFU reduces the argument itself; the error
+//    grows as |x| * 2^-24), otherwise x is reduced to [-pi, pi] first.
+#include "idg_device.cuh"
+#include "idg_internal.h"
+#include "idg_ptx.cuh"
+
+namespace idg {
+
+namespace {
+
+constexpr int kT = 128;                       // threads per CTA
+constexpr int kPairs = 4;                     // pixel pairs per thread per pass
+constexpr int kPassPairs = kT * kPairs;       // 512 pairs = 1024 pixels per pass
+constexpr int kTileVis = 256;                 // visibilities per staged tile
+constexpr int kMaxTT = 64;                    // timesteps per tile, at most
+constexpr int kMaxChunk = kTileVis;           // channels per tile, at most
+constexpr float kFastBound = 48.f;            // radians
+constexpr uint64_t kWaitNs = 2000000000ull;   // a staged copy not complete after 2 s is declared lost
+
+constexpr float kInv2Pi = 0.159154943091895335769f;
+constexpr float k2PiHi = 6.28125f;                        // 2 pi split for exact k * 2pi_hi (k < 2^15)
+constexpr float k2PiLo = 1.9353071795864769253e-3f;       // 2 pi - k2PiHi
+
+struct SmemHead {
+    uint64_t bar;
+    int fast;        // tile uses the unreduced path
+    int qmax_bits;   // max |Q| of the tile (float bits, non-negative)
+    int kmax_bits;   // max |kappa| of the subgrid
+    int abort;       // a staged copy did not arrive in time
+    int next;        // work item
+};
+
+struct Layout {
+    size_t raw, vexp, coef, kappa, geo, total;
+};
+
+__host__ __device__ inline Layout layout(int S, int C) {
+    Layout L;
+    size_t off = 64;                                   // SmemHead
+    L.raw = off;  off += (size_t)kTileVis * 32;        // raw visibilities (TMA destination)
+    L.vexp = off; off += (size_t)kTileVis * 96;        // expanded operand pairs
+    L.coef = off; off += (size_t)kMaxTT * 48;          // per timestep: (a,a,b,b) (g,g,qu,qu) (qv,qv,qw,qw)
+    L.kappa = off; off += (size_t)C * 8;               // (kappa, kappa)
+    off = (off + 15) & ~size_t(15);
+    L.geo = off;  off += (size_t)(S * S / 2) * 24;      // per pair: (hx0,hx1) (hy,hy) (n0,n1)
+    L.total = off;
+    return L;
+}
+
+__device__ __forceinline__ f2 dup(float v) { return pack2(v, v); }
+
+// x - 2 pi rint(x / 2 pi), elementwise on a pair (Cody-Waite, two constants).
+__device__ __forceinline__ f2 reduce_2pi(f2 x) {
+    const f2 M = pack2(12582912.0f, 12582912.0f);
+    f2 k = fmul2(x, pack2(kInv2Pi, kInv2Pi));
+    k = fsub2(fadd2(k, M), M);
+    x = ffma2(k, pack2(-k2PiHi, -k2PiHi), x);
+    return ffma2(k, pack2(-k2PiLo, -k2PiLo), x);
+}
+
+__device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
+    float x0, x1, s0, c0, s1, c1;
+    unpack2(x, x0, x1);
+    __sincosf(x0, &s0, &c0);
+    __sincosf(x1, &s1, &c1);
+    c = pack2(c0, c1);
+    s = pack2(s0, s1);
+}
+
+__global__ void __launch_bounds__(kT, 3) gridder_fast_kernel(KernelArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int S = a.S, S2 = S * S, npairs = S2 / 2;
+    const Layout L = layout(S, a.C);
+    SmemHead *head = reinterpret_cast<SmemHead *>(smem);
+    float4 *raw = reinterpret_cast<float4 *>(smem + L.raw);
+    float4 *vexp = reinterpret_cast<float4 *>(smem + L.vexp);
+    float4 *coef = reinterpret_cast<float4 *>(smem + L.coef);
+    f2 *kap = reinterpret_cast<f2 *>(smem + L.kappa);
+    f2 *geo = reinterpret_cast<f2 *>(smem + L.geo);
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        mbar_init(&head->bar, 1);
+        mbar_init_fence();
+        head->abort = 0;
+    }
+    // pixel geometry of every pair, once per CTA (FP64 n as in math.hpp:31-37)
+    for (int p = tid; p < npairs; p += kT) {
+        const float3 g0 = pixel_geometry(2 * p, S, a.image_size);
+        const float3 g1 = pixel_geometry(2 * p + 1, S, a.image_size);
+        geo[3 * p + 0] = pack2(g0.x, g1.x);
+        geo[3 * p + 1] = pack2(g0.y, g1.y);
+        geo[3 * p + 2] = pack2(g0.z, g1.z);
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const double d2pi = (double)a.image_size / (double)S / kTwoPi;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            head->next = atomicAdd(a.work_counter, 1);
+            head->kmax_bits = 0;
+            head->qmax_bits = 0;
+        }
+        __syncthreads();
+        const int idx = head->next;
+        if (idx >= a.nr_subgrids || head->abort) break;
+        const int s = a.work_list ? a.work_list[idx] : idx;
+        const SubgridInfo si = load_subgrid(a, s);
+        const int nc = si.c1 - si.c0;
+        if (!si.ok) {
+            if (tid == 0) flag_status(a.status, kStatusBadPlan);
+            for (int i = tid; i < 4 * S2; i += kT) a.subgrids[(size_t)s * 4 * S2 + i] = make_float2(0.f, 0.f);
+            continue;
+        }
+        // channel offsets relative to the middle channel; max |kappa|
+        const int cref = si.c0 + (nc > 0 ? (nc - 1) / 2 : 0);
+        const double kref = nc > 0 ? (double)a.wavenumbers[cref] : 0.0;
+        float kmax = 0.f;
+        for (int c = tid; c < nc; c += kT) {
+            const float kv = (float)((double)a.wavenumbers[si.c0 + c] - kref);
+            kap[c] = dup(kv);
+            kmax = fmaxf(kmax, fabsf(kv));
+        }
+        // block max of kmax through the head word (non-negative floats order as ints)
+        if (kmax > 0.f) atomicMax(&head->kmax_bits, __float_as_int(kmax));
+        __syncthreads();
+        const float kappa_max = __int_as_float(head->kmax_bits);
+
+        const int chunk = nc < kMaxChunk ? nc : kMaxChunk;
+        const int TT = nc > 0 ? min(kMaxTT, kTileVis / chunk) : 1;
+        const float hmax = 0.5f * (float)(S - 1);
+        const float3 gc = pixel_geometry(0, S, a.image_size);
+        const float nmax = gc.z;
+
+        for (int pass = 0; pass * kPassPairs < npairs; ++pass) {
+            f2 acc[kPairs][8];
+#pragma unroll
+            for (int j = 0; j < kPairs; ++j)
+#pragma unroll
+                for (int r = 0; r < 8; ++r) acc[j][r] = 0ull;
+            int pr[kPairs];
+#pragma unroll
+            for (int j = 0; j < kPairs; ++j) {
+                const int p = pass * kPassPairs + tid + j * kT;
+                pr[j] = p < npairs ? p : 0;
+            }
+
+            for (int cb = 0; cb < nc; cb += chunk) {
+                const int ncc = min(chunk, nc - cb);
+                for (int t0 = 0; t0 < si.T; t0 += TT) {
+                    const int tt = min(TT, si.T - t0);
+                    // ---- stage: bulk copies of tt rows x ncc visibilities
+                    __syncthreads(); // previous tile fully consumed (raw, vexp, coef)
+                    if (tid == 0) {
+                        const uint32_t row_bytes = (uint32_t)ncc * 32u;
+                        fence_proxy_async();
+                        mbar_arrive_expect_tx(&head->bar, row_bytes * (uint32_t)tt);
+                        const float4 *src = a.vis + ((int64_t)si.row0 + t0) * a.C * 2 + (int64_t)(si.c0 + cb) * 2;
+                        for (int r = 0; r < tt; ++r)
+                            bulk_g2s(raw + (size_t)r * ncc * 2, src + (int64_t)r * a.C * 2, row_bytes, &head->bar);
+                    }
+                    // phase coefficients (FP64) for the tile's timesteps, and max |Q|
+                    for (int t = tid; t < tt; t += kT) {
+                        const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
+                        const double u = p[0], v = p[1], w = p[2];
+                        double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
+                        double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
+                        ca -= 2.0 * rint(ca * 0.5);
+                        cbv -= 2.0 * rint(cbv * 0.5);
+                        const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
+                        const float A = (float)(kTwoPi * ca), B = (float)(kTwoPi * cbv), Gv = (float)cg;
+                        const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
+                        coef[3 * t + 0] = make_float4(A, A, B, B);
+                        coef[3 * t + 1] = make_float4(Gv, Gv, qu, qu);
+                        coef[3 * t + 2] = make_float4(qv, qv, qw, qw);
+                        const float qm = fabsf(qu) * hmax + fabsf(qv) * hmax + fabsf(qw) * nmax;
+                        atomicMax(&head->qmax_bits, __float_as_int(qm));
+                    }
+                    // ---- wait for the copies, expand into operand pairs
+                    if (!mbar_wait_bounded(&head->bar, phase, kWaitNs)) {
+                        head->abort = 1;
+                        flag_status(a.status, kStatusTimeout);
+                    }
+                    __syncthreads();
+                    if (head->abort) {
+                        // give the copies in flight one more bounded wait before the CTA exits
+                        if (tid == 0) mbar_wait_bounded(&head->bar, phase, kWaitNs);
+                        break;
+                    }
+                    phase ^= 1u;
+                    for (int i = tid; i < tt * ncc; i += kT) {
+                        const float4 v0 = raw[2 * i], v1 = raw[2 * i + 1];
+                        float4 *d = vexp + 6 * i;
+                        d[0] = make_float4(v0.x, v0.x, v0.y, v0.y);
+                        d[1] = make_float4(v0.z, v0.z, v0.w, v0.w);
+                        d[2] = make_float4(v1.x, v1.x, v1.y, v1.y);
+                        d[3] = make_float4(v1.z, v1.z, v1.w, v1.w);
+                        d[4] = make_float4(-v0.y, -v0.y, -v0.w, -v0.w);
+                        d[5] = make_float4(-v1.y, -v1.y, -v1.w, -v1.w);
+                    }
+                    if (tid == 0) {
+                        head->fast = (3.1416f + kappa_max * __int_as_float(head->qmax_bits)) <= kFastBound ? 1 : 0;
+                        head->qmax_bits = 0; // next tile's atomics come after two more barriers
+                    }
+                    __syncthreads();
+                    const bool fast = head->fast != 0;
+
+                    // ---- compute
+                    for (int t = 0; t < tt; ++t) {
+                        const float4 c0 = coef[3 * t], c1 = coef[3 * t + 1], c2 = coef[3 * t + 2];
+                        const f2 A2 = pack2(c0.x, c0.y), B2 = pack2(c0.z, c0.w), G2 = pack2(c1.x, c1.y);
+                        const f2 QU = pack2(c1.z, c1.w), QV = pack2(c2.x, c2.y), QW = pack2(c2.z, c2.w);
+                        f2 tau0[kPairs], Q[kPairs];
+#pragma unroll
+                        for (int j = 0; j < kPairs; ++j) {
+                            const f2 hx = geo[3 * pr[j]], hy = geo[3 * pr[j] + 1], nn = geo[3 * pr[j] + 2];
+                            tau0[j] = reduce_2pi(ffma2(A2, hx, ffma2(B2, hy, fmul2(G2, nn))));
+                            Q[j] = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
+                        }
+                        const float4 *vt = vexp + (size_t)t * ncc * 6;
+                        const f2 *kp = kap + cb;
+#pragma unroll 1
+                        for (int c = 0; c < ncc; ++c) {
+                            const f2 kc = kp[c];
+                            const float4 *vv = vt + 6 * c;
+                            const float4 e0 = vv[0], e1 = vv[1], e2 = vv[2], e3 = vv[3], e4 = vv[4], e5 = vv[5];
+                            const f2 vr0 = pack2(e0.x, e0.y), vi0 = pack2(e0.z, e0.w);
+                            const f2 vr1 = pack2(e1.x, e1.y), vi1 = pack2(e1.z, e1.w);
+                            const f2 vr2 = pack2(e2.x, e2.y), vi2 = pack2(e2.z, e2.w);
+                            const f2 vr3 = pack2(e3.x, e3.y), vi3 = pack2(e3.z, e3.w);
+                            const f2 ni0 = pack2(e4.x, e4.y), ni1 = pack2(e4.z, e4.w);
+                            const f2 ni2 = pack2(e5.x, e5.y), ni3 = pack2(e5.z, e5.w);
+#pragma unroll
+                            for (int j = 0; j < kPairs; ++j) {
+                                f2 x = ffma2(kc, Q[j], tau0[j]);
+                                if (!fast) x = reduce_2pi(x);
+                                f2 C, Sn;
+                                sincos_pair(x, C, Sn);
+                                // P += V * (cos + i sin): re += vr c - vi s ; im += vr s + vi c
+                                acc[j][0] = ffma2(ni0, Sn, ffma2(vr0, C, acc[j][0]));
+                                acc[j][1] = ffma2(vi0, C, ffma2(vr0, Sn, acc[j][1]));
+                                acc[j][2] = ffma2(ni1, Sn, ffma2(vr1, C, acc[j][2]));
+                                acc[j][3] = ffma2(vi1, C, ffma2(vr1, Sn, acc[j][3]));
+                                acc[j][4] = ffma2(ni2, Sn, ffma2(vr2, C, acc[j][4]));
+                                acc[j][5] = ffma2(vi2, C, ffma2(vr2, Sn, acc[j][5]));
+                                acc[j][6] = ffma2(ni3, Sn, ffma2(vr3, C, acc[j][6]));
+                                acc[j][7] = ffma2(vi3, C, ffma2(vr3, Sn, acc[j][7]));
+                            }
+                        }
+                    }
+                }
+                if (head->abort) break;
+            }
+            if (head->abort) break;
+
+            // ---- epilogue: A-terms, taper, store two pixels per pair
+            const size_t jones_stride = (size_t)S2 * 2;
+            const float4 *a1 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st1) * jones_stride;
+            const float4 *a2 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st2) * jones_stride;
+            const bool taper = (a.flags & IDG_FLAG_NO_TAPER) == 0;
+#pragma unroll
+            for (int j = 0; j < kPairs; ++j) {
+                const int p = pass * kPassPairs + tid + j * kT;
+                if (p >= npairs) continue;
+                cf px[2][4];
+#pragma unroll
+                for (int pol = 0; pol < 4; ++pol) {
+                    float r0, r1, i0, i1;
+                    unpack2(acc[j][2 * pol], r0, r1);
+                    unpack2(acc[j][2 * pol + 1], i0, i1);
+                    px[0][pol] = {r0, i0};
+                    px[1][pol] = {r1, i1};
+                }
+                float out[2][8];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int q = 2 * p + h;
+                    cf j1[4], j2[4];
+                    load_jones(a1 + 2 * q, j1);
+                    load_jones(a2 + 2 * q, j2);
+                    aterm_gridder(px[h], j1, j2);
+                    const float sph = taper ? a.taper[q] : 1.f;
+#pragma unroll
+                    for (int pol = 0; pol < 4; ++pol) {
+                        out[h][2 * pol] = px[h][pol].re * sph;
+                        out[h][2 * pol + 1] = px[h][pol].im * sph;
+                    }
+                }
+#pragma unroll
+                for (int pol = 0; pol < 4; ++pol) {
+                    float4 *dst = reinterpret_cast<float4 *>(a.subgrids + ((size_t)s * 4 + pol) * S2 + 2 * p);
+                    *dst = make_float4(out[0][2 * pol], out[0][2 * pol + 1], out[1][2 * pol], out[1][2 * pol + 1]);
+                }
+            }
+        }
+        if (head->abort) break;
+    }
+}
+
+} // namespace
+
+size_t gridder_fast_smem(int S, int C) { return layout(S, C).total; }
+
+cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream) {
+    const size_t smem = layout(a.S, a.C).total;
+    cudaError_t e = cudaFuncSetAttribute(gridder_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gridder_fast_kernel, kT, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
+    gridder_fast_kernel<<<(unsigned)blocks, kT, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace idg

@@ -8,8 +8,12 @@ namespace idg {
 
 struct KernelArgs;
 
+// IDG_VARIANT_PLAIN: one CTA per subgrid (idg_gridder.cu / idg_degridder.cu).
+// IDG_VARIANT_BATCHED: persistent packed-FP32x2 kernels (idg_*_fast.cu); need a.work_counter.
 cudaError_t launch_gridder(const KernelArgs &a, int variant, int max_nc, cudaStream_t stream);
 cudaError_t launch_degridder(const KernelArgs &a, int variant, int max_nc, cudaStream_t stream);
+cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream);
+cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream);
 
 bool fft_size_supported(int S);
 cudaError_t launch_subgrid_fft(float2 *data, int64_t nr_subgrids, int S, int direction, const float *taper,

@@ -62,6 +62,7 @@ class ObservationSpec:
     aterm_interval: int = 0    # timesteps per A-term slot (0 -> one slot)
     seed: int = 1234
     taper_c: float = 3.0 * np.pi
+    subgrid_limit: int = 0     # > 0: only the plan's first subgrid_limit subgrids (and their rows) are used
 
     @property
     def n_baselines(self) -> int:
@@ -73,10 +74,15 @@ class ObservationSpec:
 
     @property
     def n_subgrids(self) -> int:
-        return self.n_baselines * self.subgrids_per_baseline
+        n = self.n_baselines * self.subgrids_per_baseline
+        return min(n, self.subgrid_limit) if self.subgrid_limit > 0 else n
 
     @property
     def n_rows(self) -> int:
+        if self.subgrid_limit > 0:
+            last = self.n_subgrids - 1
+            bl, ts = divmod(last, self.subgrids_per_baseline)
+            return bl * self.ntimesteps + (ts + 1) * self.timesteps_per_subgrid
         return self.n_baselines * self.ntimesteps
 
     @property
@@ -222,6 +228,19 @@ def make_observation(spec: ObservationSpec) -> Observation:
     taper = pswf_taper(S, spec.taper_c)
     md = plan_subgrids(spec, uvw, freqs, bl)
     return Observation(spec, st, bl, uvw, freqs, k, at, taper, md)
+
+
+def truncate_observation(obs: Observation, max_subgrids: int) -> Observation:
+    """The first `max_subgrids` subgrids of the plan and the rows they use
+    (whole baselines first, so the rows stay contiguous)."""
+    import dataclasses
+
+    keep = max(1, min(max_subgrids, obs.spec.n_subgrids))
+    spec = dataclasses.replace(obs.spec, subgrid_limit=keep)
+    md = obs.metadata[:keep].copy()
+    rows = spec.n_rows
+    return Observation(spec, obs.stations, obs.baselines, np.ascontiguousarray(obs.uvw[:rows]), obs.frequencies,
+                       obs.wavenumbers, obs.aterms, obs.taper, md)
 
 
 def visibilities(spec: ObservationSpec, device="cpu", seed: int | None = None):

@@ -68,3 +68,11 @@ def rel_rms(x, ref):
     ref = np.asarray(ref, np.complex128)
     den = np.linalg.norm(ref)
     return float(np.linalg.norm(x - ref) / (den if den > 0 else 1.0))
+
+
+def check_rel(name, x, ref, tol):
+    """Relative RMS check that also prints the measured error (visible with pytest -s)."""
+    e = rel_rms(x, ref)
+    print(f"[parity] {name}: relative RMS {e:.3e} (tolerance {tol:.0e})")
+    assert e <= tol, f"{name}: relative RMS {e:.3e} > {tol:.0e}"
+    return e

@@ -10,7 +10,7 @@ import pytest
 import torch
 
 import idg_gb300._lib as L
-from conftest import golden_cases, load_golden, rel_rms
+from conftest import check_rel, golden_cases, load_golden, rel_rms
 from gpu_helpers import degrid_gpu, dev, grid_gpu, spec_for
 
 pytestmark = pytest.mark.gpu
@@ -44,7 +44,7 @@ def test_gridder_config1_vs_fp64(oracle_mod, idg, variant):
     prm = oracle_mod.params(spec.grid_size, spec.subgrid_size, spec.nchannels, spec.nstations, spec.n_subgrids,
                             spec.image_size)
     want = oracle_mod.gridder(prm, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, obs.metadata)
-    assert rel_rms(got, want) <= TOL
+    check_rel(f"gridder config1 v{variant}", got, want, TOL)
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
@@ -60,7 +60,7 @@ def test_degridder_config1_vs_fp64(oracle_mod, idg, variant, refcpu):
     prm = oracle_mod.params(spec.grid_size, S, spec.nchannels, spec.nstations, spec.n_subgrids, spec.image_size)
     want = oracle_mod.degridder(prm, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, obs.metadata, spec.n_rows,
                                 aterm_mode=oracle_mod.ATERM_REFCPU if refcpu else oracle_mod.ATERM_ADJOINT)
-    assert rel_rms(got, want) <= TOL
+    check_rel(f"degridder config1 v{variant} refcpu={refcpu}", got, want, TOL)
 
 
 @pytest.mark.parametrize("path", golden_cases(), ids=lambda p: p.rsplit("/", 1)[-1])
@@ -75,13 +75,13 @@ def test_reference_inputs_gridder_and_degridder(oracle_mod, idg, path):
     for variant in VARIANTS:
         got = grid_gpu(sp, d["metadata"], d["uvw"], d["wavenumbers"], d["vis"], d["spheroidal"], d["aterms"], variant)
         want = oracle_mod.gridder(prm, d["uvw"], d["wavenumbers"], d["vis"], d["spheroidal"], d["aterms"], d["metadata"])
-        assert rel_rms(got, want) <= TOL
+        check_rel(f"gridder reference-inputs v{variant}", got, want, TOL)
         assert rel_rms(d["gridder_out"], got) < 5e-4
         vg = degrid_gpu(sp, d["metadata"], d["uvw"], d["wavenumbers"], d["degridder_in"], d["spheroidal"],
                         d["aterms"], d["vis"].shape[0], variant)
         vw = oracle_mod.degridder(prm, d["uvw"], d["wavenumbers"], d["degridder_in"], d["spheroidal"], d["aterms"],
                                   d["metadata"], d["vis"].shape[0], aterm_mode=oracle_mod.ATERM_REFCPU)
-        assert rel_rms(vg, vw) <= TOL
+        check_rel(f"degridder reference-inputs v{variant}", vg, vw, TOL)
         assert rel_rms(d["degridder_out"], vg) < 5e-4
 
 
@@ -108,12 +108,12 @@ def test_config2_sample_vs_fp64(oracle_mod, idg):
     want = oracle_mod.gridder(prm, uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, md)
     for variant in VARIANTS:
         got = grid_gpu(sp, md, uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, variant)
-        assert rel_rms(got, want) <= TOL
+        check_rel(f"gridder config2-sample v{variant}", got, want, TOL)
     sub = (rng.standard_normal((len(md), 4, S, S)) + 1j * rng.standard_normal((len(md), 4, S, S))).astype(np.complex64)
     vwant = oracle_mod.degridder(prm, uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, md, len(rows))
     for variant in VARIANTS:
         vgot = degrid_gpu(sp, md, uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, len(rows), variant)
-        assert rel_rms(vgot, vwant) <= TOL
+        check_rel(f"degridder config2-sample v{variant}", vgot, vwant, TOL)
 
 
 @pytest.mark.parametrize("S", [8, 16, 24, 32, 48, 64])
@@ -179,3 +179,97 @@ def test_bad_plan_entry_is_flagged_not_faulted(idg):
     assert np.all(got[3] == 0) and np.all(got[5] == 0)
     assert np.any(got[4] != 0)
     assert ops.device_status(clear=True) == 0
+
+
+def _oracle_with_ext(oracle_mod, G, S, ns, image_size, uvw, k, vis, taper, aterms, md, ext, sub_in=None, w_step=0.0):
+    """FP64 oracle for plans whose subgrids cover channel ranges [c0, c1): one oracle
+    call per distinct range on the sliced channel axis."""
+    N, C = md.shape[0], k.shape[0]
+    grid_out = np.zeros((N, 4, S, S), np.complex128)
+    vis_out = np.zeros((vis.shape[0], C, 4), np.complex128)
+    for c0, c1 in sorted(set(zip(ext["channel_begin"].tolist(), ext["channel_end"].tolist()))):
+        sel = np.where((ext["channel_begin"] == c0) & (ext["channel_end"] == c1))[0]
+        if c1 <= c0:
+            continue
+        prm = oracle_mod.params(G, S, c1 - c0, ns, len(sel), image_size, w_step)
+        kk = np.ascontiguousarray(k[c0:c1])
+        vv = np.ascontiguousarray(vis[:, c0:c1])
+        mds = np.ascontiguousarray(md[sel])
+        # the oracle reads rows relative to the first entry's baseline_offset (all zero here)
+        grid_out[sel] = oracle_mod.gridder(prm, uvw, kk, vv, taper, aterms, mds)
+        if sub_in is not None:
+            part = oracle_mod.degridder(prm, uvw, kk, np.ascontiguousarray(sub_in[sel]), taper, aterms, mds,
+                                        vis.shape[0])
+            for m in mds:
+                r0, r1 = m["time_offset"], m["time_offset"] + m["nr_timesteps"]
+                vis_out[r0:r1, c0:c1] = part[r0:r1]
+    return grid_out, vis_out
+
+
+@pytest.mark.parametrize("S", [24, 48, 64])
+def test_uneven_plan_channel_groups(oracle_mod, idg, S):
+    """Uneven subgrids in one launch: random timesteps per subgrid, channel ranges from
+    the sidecar, non-overlapping rows; subgrid sizes needing 1, 3 and 4 pixel passes."""
+    from idg_gb300 import datasets as D
+
+    rng = np.random.default_rng(100 + S)
+    G, C, ns = 2048, 24, 6
+    image_size = 0.04
+    spec = D.ObservationSpec(nstations=ns, disk_radius_m=2500.0, ntimesteps=160, timesteps_per_subgrid=160,
+                             nchannels=C, f_start=140e6, f_end=170e6, subgrid_size=S, grid_size=G,
+                             image_size=image_size, aterm_sigma=0.05, seed=S)
+    obs = D.make_observation(spec)
+    N = 20
+    T = rng.integers(5, 41, N)
+    md = np.zeros(N, L.METADATA_DTYPE)
+    md["time_offset"] = np.concatenate([[0], np.cumsum(T)[:-1]])
+    md["nr_timesteps"] = T
+    md["station1"] = rng.integers(0, ns - 1, N)
+    md["station2"] = md["station1"] + 1
+    md["x"] = rng.integers(0, G - S, N)
+    md["y"] = rng.integers(0, G - S, N)
+    lens = rng.choice([3, 8, 16, 24], N)
+    c0 = np.array([rng.integers(0, C - L_ + 1) for L_ in lens])
+    ext = np.zeros(N, L.SUBGRID_EXT_DTYPE)
+    ext["channel_begin"] = c0
+    ext["channel_end"] = c0 + lens
+    rows = int(T.sum())
+    uvw = np.ascontiguousarray(obs.uvw[:rows])
+    vis = (rng.standard_normal((rows, C, 4)) + 1j * rng.standard_normal((rows, C, 4))).astype(np.complex64)
+    sub_in = (rng.standard_normal((N, 4, S, S)) + 1j * rng.standard_normal((N, 4, S, S))).astype(np.complex64)
+    want_g, want_v = _oracle_with_ext(oracle_mod, G, S, ns, image_size, uvw, obs.wavenumbers, vis, obs.taper,
+                                      obs.aterms, md, ext, sub_in)
+    sp = spec_for(G, S, C, ns, obs.aterms.shape[0], image_size)
+    covered = np.zeros((rows, C), bool)
+    for m, e in zip(md, ext):
+        covered[m["time_offset"]:m["time_offset"] + m["nr_timesteps"], e["channel_begin"]:e["channel_end"]] = True
+    for variant in VARIANTS:
+        got = grid_gpu(sp, md, uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, variant, ext=ext)
+        check_rel(f"gridder uneven S={S} v{variant}", got, want_g, TOL)
+        vg = degrid_gpu(sp, md, uvw, obs.wavenumbers, sub_in, obs.taper, obs.aterms, rows, variant, ext=ext)
+        check_rel(f"degridder uneven S={S} v{variant}", vg[covered], want_v[covered], TOL)
+        assert np.all(vg[~covered] == 0)
+
+
+def test_large_phase_path(oracle_mod, idg):
+    """Subgrids whose per-channel phase exceeds the unreduced-sincos bound take the
+    reduced path in the batched kernels; both variants stay within tolerance."""
+    from idg_gb300 import datasets as D
+
+    spec = D.ObservationSpec(nstations=5, disk_radius_m=10000.0, ntimesteps=32, timesteps_per_subgrid=32,
+                             nchannels=16, f_start=150e6, f_end=170e6, subgrid_size=64, grid_size=4096,
+                             image_size=0.05, seed=9)
+    obs = D.make_observation(spec)
+    vis = _vis(spec, seed=3)
+    sp = spec_for(spec.grid_size, 64, 16, 5, 1, spec.image_size)
+    prm = oracle_mod.params(spec.grid_size, 64, 16, 5, spec.n_subgrids, spec.image_size)
+    want = oracle_mod.gridder(prm, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, obs.metadata)
+    for variant in VARIANTS:
+        got = grid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, variant)
+        check_rel(f"gridder large-phase v{variant}", got, want, TOL)
+    rng = np.random.default_rng(4)
+    sub = (rng.standard_normal((spec.n_subgrids, 4, 64, 64)) + 1j * rng.standard_normal((spec.n_subgrids, 4, 64, 64))).astype(np.complex64)
+    vwant = oracle_mod.degridder(prm, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, obs.metadata, spec.n_rows)
+    for variant in VARIANTS:
+        vgot = degrid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, spec.n_rows, variant)
+        check_rel(f"degridder large-phase v{variant}", vgot, vwant, TOL)
