@@ -126,6 +126,21 @@ IDG_API int idg_gridder(const idg_params *params, int variant, int64_t nr_subgri
                         const float *uvw, const float *wavenumbers, const void *visibilities,
                         const float *spheroidal, const void *aterms, void *subgrids, void *stream);
 
+/* The batched gridder (IDG_VARIANT_BATCHED of idg_gridder), for callers that
+ * may not allocate device memory.  No counterpart in the reference.
+ * idg_gridder() obtains its two scratch words (work counter, check word) with
+ * cudaMalloc on first use; this entry point keeps them in a 256-byte static
+ * device array of the library instead and calls no allocator.  Same arguments
+ * and result as idg_gridder().  Limits: at most 2^30 subgrids; calls on one
+ * device share the array, so calls whose kernels could overlap on the GPU
+ * must be serialised by the caller; a rejected plan entry yields a zero
+ * subgrid (its check bit is not reported).  The first call on a device looks
+ * up the array's address and should come before any stream capture there. */
+IDG_API int idg_gridder_noalloc(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                                const idg_subgrid_ext *ext, int64_t nr_rows, const float *uvw,
+                                const float *wavenumbers, const void *visibilities, const float *spheroidal,
+                                const void *aterms, void *subgrids, void *stream);
+
 /* Degridder: V[t,c] = sum_pixels A(taper * subgrid) e^{-i phi}; writes only
  * the rows/channels the plan names.  Replaces kernel_degridder_v6
  * (gridding/src/degridding_benchmark.cu:106-203) and the CPU loops of

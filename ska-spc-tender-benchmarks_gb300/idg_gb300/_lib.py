@@ -115,6 +115,7 @@ _SIGNATURES = {
     "idg_last_error": [],
     "idg_device_status": [_P, ctypes.POINTER(ctypes.c_uint32), _I32],
     "idg_gridder": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
+    "idg_gridder_noalloc": [ctypes.POINTER(IdgParams), _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
     "idg_degridder": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
     "idg_subgrid_fft": [ctypes.POINTER(IdgParams), _I64, _I32, _P, _P, _P],
     "idg_adder": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
