@@ -269,6 +269,27 @@ IDG_API int idg_reference_dataset(int64_t grid_size, int64_t subgrid_size, int64
                                   float *uvw, float *frequencies, float *wavenumbers, void *visibilities,
                                   uint32_t *baselines, float *spheroidal, void *aterms, idg_metadata *metadata);
 
+/* ------------------------------------------------------------------ */
+/* Launch shapes of the batched kernels and their autotuner            */
+/* ------------------------------------------------------------------ */
+/* The batched gridder and degridder are compiled in several launch shapes
+ * (threads per CTA, pixel pairs per thread, staging tile, CTAs per SM).  The
+ * shape used for a subgrid size on the current device is 0 until set here or
+ * by idg_autotune().  No counterpart in the reference. */
+IDG_API int idg_batched_shapes(int *gridder_shapes, int *degridder_shapes);
+IDG_API int idg_set_batched_shapes(int subgrid_size, int gridder_shape, int degridder_shape);
+IDG_API int idg_get_batched_shapes(int subgrid_size, int *gridder_shape, int *degridder_shape);
+/* Times every shape of both batched kernels on the given (device) plan and
+ * data -- writes `subgrids` and `visibilities_out` -- and selects the fastest
+ * for params->subgrid_size on the current device.  gridder_ms / degridder_ms
+ * receive the mean time of each shape (arrays of the sizes idg_batched_shapes
+ * reports).  Synchronises `stream`. */
+IDG_API int idg_autotune(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                         const idg_subgrid_ext *ext, int64_t nr_rows, const float *uvw, const float *wavenumbers,
+                         const void *visibilities, const float *spheroidal, const void *aterms, void *subgrids,
+                         void *visibilities_out, void *stream, int repeats, double *gridder_ms,
+                         double *degridder_ms, int *best_gridder, int *best_degridder);
+
 /* Reports the peak FP32 FMA rate of the current device measured by a short
  * dependent-chain microbenchmark (flop/s, 2 flop per FMA). */
 IDG_API int idg_measure_fp32_peak(double *flops_per_second);

@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -28,7 +29,39 @@ namespace {
 thread_local std::string g_last_error;
 std::mutex g_words_mutex;
 std::vector<DeviceWords> g_words;
+
+// Launch shapes of the batched kernels per (device, subgrid size), set by the
+// autotuner or by idg_set_batched_shapes(); shape 0 until then.
+std::mutex g_shape_mutex;
+std::map<std::pair<int, int>, std::pair<int, int>> g_shapes;
+
+int current_device() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev;
+}
 } // namespace
+
+int batched_gridder_shape(int S) {
+    std::lock_guard<std::mutex> lock(g_shape_mutex);
+    auto it = g_shapes.find({current_device(), S});
+    return it == g_shapes.end() ? 0 : it->second.first;
+}
+int batched_degridder_shape(int S) {
+    std::lock_guard<std::mutex> lock(g_shape_mutex);
+    auto it = g_shapes.find({current_device(), S});
+    return it == g_shapes.end() ? 0 : it->second.second;
+}
+void set_batched_gridder_shape(int S, int shape) {
+    std::lock_guard<std::mutex> lock(g_shape_mutex);
+    auto &v = g_shapes[{current_device(), S}];
+    v.first = shape;
+}
+void set_batched_degridder_shape(int S, int shape) {
+    std::lock_guard<std::mutex> lock(g_shape_mutex);
+    auto &v = g_shapes[{current_device(), S}];
+    v.second = shape;
+}
 
 int fail(int code, const char *fmt, ...) {
     char buf[1024];
@@ -406,6 +439,93 @@ IDG_API int idg_reference_dataset(int64_t grid_size, int64_t subgrid_size, int64
     return reference_dataset(grid_size, subgrid_size, nstations, nchannels, ntimeslots, ntimesteps_per_subgrid,
                              image_size, uvw, frequencies, wavenumbers, visibilities, baselines, spheroidal, aterms,
                              metadata);
+}
+
+IDG_API int idg_batched_shapes(int *gridder_shapes, int *degridder_shapes) {
+    if (!gridder_shapes || !degridder_shapes) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL output");
+    *gridder_shapes = gridder_fast_shapes();
+    *degridder_shapes = degridder_fast_shapes();
+    return IDG_OK;
+}
+
+IDG_API int idg_set_batched_shapes(int subgrid_size, int gridder_shape, int degridder_shape) {
+    if (gridder_shape < 0 || gridder_shape >= gridder_fast_shapes() || degridder_shape < 0 ||
+        degridder_shape >= degridder_fast_shapes())
+        return fail(IDG_ERR_INVALID_ARGUMENT, "shape out of range (gridder %d of %d, degridder %d of %d)", gridder_shape,
+                    gridder_fast_shapes(), degridder_shape, degridder_fast_shapes());
+    set_batched_gridder_shape(subgrid_size, gridder_shape);
+    set_batched_degridder_shape(subgrid_size, degridder_shape);
+    return IDG_OK;
+}
+
+IDG_API int idg_get_batched_shapes(int subgrid_size, int *gridder_shape, int *degridder_shape) {
+    if (!gridder_shape || !degridder_shape) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL output");
+    *gridder_shape = batched_gridder_shape(subgrid_size);
+    *degridder_shape = batched_degridder_shape(subgrid_size);
+    return IDG_OK;
+}
+
+IDG_API int idg_autotune(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                         const idg_subgrid_ext *ext, int64_t nr_rows, const float *uvw, const float *wavenumbers,
+                         const void *visibilities, const float *spheroidal, const void *aterms, void *subgrids,
+                         void *visibilities_out, void *stream, int repeats, double *gridder_ms, double *degridder_ms,
+                         int *best_gridder, int *best_degridder) {
+    if (!gridder_ms || !degridder_ms || !best_gridder || !best_degridder || !visibilities_out)
+        return fail(IDG_ERR_INVALID_ARGUMENT, "NULL output");
+    if (repeats < 1) repeats = 1;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    EventPair ev;
+    if (int rc = ev.create()) return rc;
+    const int S = params ? params->subgrid_size : 0;
+    const int g0 = batched_gridder_shape(S), d0 = batched_degridder_shape(S);
+    double best_g = 1e300, best_d = 1e300;
+    *best_gridder = g0;
+    *best_degridder = d0;
+    for (int sh = 0; sh < gridder_fast_shapes(); ++sh) {
+        set_batched_gridder_shape(S, sh);
+        int rc = idg_gridder(params, IDG_VARIANT_BATCHED, nr_subgrids, metadata, ext, nr_rows, uvw, wavenumbers,
+                             visibilities, spheroidal, aterms, subgrids, stream); // warm-up
+        if (rc) {
+            set_batched_gridder_shape(S, g0);
+            return rc;
+        }
+        IDG_CUDA(cudaEventRecord(ev.a, st));
+        for (int r = 0; r < repeats; ++r)
+            idg_gridder(params, IDG_VARIANT_BATCHED, nr_subgrids, metadata, ext, nr_rows, uvw, wavenumbers,
+                        visibilities, spheroidal, aterms, subgrids, stream);
+        IDG_CUDA(cudaEventRecord(ev.b, st));
+        float ms = 0;
+        if (int rc2 = ev.elapsed_ms(&ms)) return rc2;
+        gridder_ms[sh] = ms / repeats;
+        if (gridder_ms[sh] < best_g) {
+            best_g = gridder_ms[sh];
+            *best_gridder = sh;
+        }
+    }
+    set_batched_gridder_shape(S, *best_gridder);
+    for (int sh = 0; sh < degridder_fast_shapes(); ++sh) {
+        set_batched_degridder_shape(S, sh);
+        int rc = idg_degridder(params, IDG_VARIANT_BATCHED, nr_subgrids, metadata, ext, nr_rows, uvw, wavenumbers,
+                               visibilities_out, spheroidal, aterms, subgrids, stream);
+        if (rc) {
+            set_batched_degridder_shape(S, d0);
+            return rc;
+        }
+        IDG_CUDA(cudaEventRecord(ev.a, st));
+        for (int r = 0; r < repeats; ++r)
+            idg_degridder(params, IDG_VARIANT_BATCHED, nr_subgrids, metadata, ext, nr_rows, uvw, wavenumbers,
+                          visibilities_out, spheroidal, aterms, subgrids, stream);
+        IDG_CUDA(cudaEventRecord(ev.b, st));
+        float ms = 0;
+        if (int rc2 = ev.elapsed_ms(&ms)) return rc2;
+        degridder_ms[sh] = ms / repeats;
+        if (degridder_ms[sh] < best_d) {
+            best_d = degridder_ms[sh];
+            *best_degridder = sh;
+        }
+    }
+    set_batched_degridder_shape(S, *best_degridder);
+    return IDG_OK;
 }
 
 IDG_API int idg_measure_fp32_peak(double *flops_per_second) {

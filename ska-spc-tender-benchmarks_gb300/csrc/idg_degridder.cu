@@ -176,7 +176,7 @@ cudaError_t launch_degridder(const KernelArgs &a, int variant, int max_nc, cudaS
         degridder_plain_kernel<<<(unsigned)a.nr_subgrids, kThreads, smem, stream>>>(a);
         return cudaGetLastError();
     }
-    return launch_degridder_fast(a, stream);
+    return launch_degridder_fast(a, stream, batched_degridder_shape(a.S));
 }
 
 } // namespace idg

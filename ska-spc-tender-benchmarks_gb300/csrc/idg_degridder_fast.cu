@@ -25,11 +25,9 @@ namespace idg {
 
 namespace {
 
-constexpr int kT = 128;
 constexpr int kCB = 4;                  // channels per group (one per lane of the group at write-out)
 constexpr int kLanesPerGroup = 4;
 constexpr int kGroupsPerWarp = 32 / kLanesPerGroup;
-constexpr int kBatchPairs = 512;        // pixel pairs staged per batch (1024 pixels)
 constexpr int kTimeTile = 64;
 constexpr float kFastBound = 48.f;
 
@@ -45,10 +43,10 @@ struct Layout {
     size_t pix, geo, coef, kappa, total;
 };
 
-__host__ __device__ inline Layout layout(int S, int C) {
+__host__ __device__ inline Layout layout(int S, int C, int batch_pairs) {
     Layout L;
     size_t off = 64;
-    L.pix = off;   off += (size_t)kBatchPairs * 96;          // 4 x (re_a,re_b,im_a,im_b) + 2 x (-re pairs)
+    L.pix = off;   off += (size_t)batch_pairs * 96;          // 4 x (re_a,re_b,im_a,im_b) + 2 x (-re pairs)
     L.geo = off;   off += (size_t)(S * S / 2) * 24;          // (hx_a,hx_b) (hy,hy) (n_a,n_b)
     L.coef = off;  off += (size_t)kTimeTile * 48;            // (a,a,b,b) (g,g,qu,qu) (qv,qv,qw,qw)
     L.kappa = off; off += (size_t)(C + kCB) * 4;             // kappa per channel, padded with zeros
@@ -73,10 +71,14 @@ __device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
     s = pack2(s0, s1);
 }
 
-__global__ void __launch_bounds__(kT, 3) degridder_fast_kernel(KernelArgs a) {
+// Kernel shape: NT threads per CTA, BATCH pixel pairs staged per pass, at least
+// MINB CTAs per SM (register cap).
+template <int NT, int BATCH, int MINB>
+__global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) {
+    constexpr int kT = NT, kBatchPairs = BATCH;
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = a.S, S2 = S * S, npairs = S2 / 2;
-    const Layout L = layout(S, a.C);
+    const Layout L = layout(S, a.C, BATCH);
     Head *head = reinterpret_cast<Head *>(smem);
     float4 *pix = reinterpret_cast<float4 *>(smem + L.pix);
     f2 *geo = reinterpret_cast<f2 *>(smem + L.geo);
@@ -275,22 +277,36 @@ __global__ void __launch_bounds__(kT, 3) degridder_fast_kernel(KernelArgs a) {
     }
 }
 
-} // namespace
-
-cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream) {
-    const size_t smem = layout(a.S, a.C).total;
-    cudaError_t e = cudaFuncSetAttribute(degridder_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int NT, int BATCH, int MINB>
+cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
+    auto kern = degridder_fast_kernel<NT, BATCH, MINB>;
+    const size_t smem = layout(a.S, a.C, BATCH).total;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, degridder_fast_kernel, kT, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
     if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
-    degridder_fast_kernel<<<(unsigned)blocks, kT, smem, stream>>>(a);
+    kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
     return cudaGetLastError();
+}
+
+} // namespace
+
+// Launch shapes of the batched degridder (index = shape id).
+int degridder_fast_shapes() { return 4; }
+
+cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
+    switch (shape) {
+    case 1: return launch_shape<128, 512, 4>(a, stream); // 16 warps/SM, register cap 128
+    case 2: return launch_shape<256, 512, 2>(a, stream); // 16 warps/SM in 256-thread CTAs
+    case 3: return launch_shape<128, 256, 4>(a, stream); // smaller staging batches
+    default: return launch_shape<128, 512, 3>(a, stream); // 12 warps/SM
+    }
 }
 
 } // namespace idg

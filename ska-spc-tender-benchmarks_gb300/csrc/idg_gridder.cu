@@ -161,7 +161,7 @@ cudaError_t launch_gridder(const KernelArgs &a, int variant, int max_nc, cudaStr
         gridder_plain_kernel<<<(unsigned)a.nr_subgrids, kThreads, smem, stream>>>(a);
         return cudaGetLastError();
     }
-    return launch_gridder_fast(a, stream);
+    return launch_gridder_fast(a, stream, batched_gridder_shape(a.S));
 }
 
 } // namespace idg

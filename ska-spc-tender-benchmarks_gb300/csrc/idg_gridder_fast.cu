@@ -27,12 +27,8 @@ namespace idg {
 
 namespace {
 
-constexpr int kT = 128;                       // threads per CTA
-constexpr int kPairs = 4;                     // pixel pairs per thread per pass
-constexpr int kPassPairs = kT * kPairs;       // 512 pairs = 1024 pixels per pass
-constexpr int kTileVis = 256;                 // visibilities per staged tile
+constexpr int kMaxTileVis = 256;              // visibilities per staged tile, at most
 constexpr int kMaxTT = 64;                    // timesteps per tile, at most
-constexpr int kMaxChunk = kTileVis;           // channels per tile, at most
 constexpr float kFastBound = 48.f;            // radians
 constexpr uint64_t kWaitNs = 2000000000ull;   // a staged copy not complete after 2 s is declared lost
 
@@ -53,11 +49,11 @@ struct Layout {
     size_t raw, vexp, coef, kappa, geo, total;
 };
 
-__host__ __device__ inline Layout layout(int S, int C) {
+__host__ __device__ inline Layout layout(int S, int C, int tile_vis) {
     Layout L;
     size_t off = 64;                                   // SmemHead
-    L.raw = off;  off += (size_t)kTileVis * 32;        // raw visibilities (TMA destination)
-    L.vexp = off; off += (size_t)kTileVis * 96;        // expanded operand pairs
+    L.raw = off;  off += (size_t)tile_vis * 32;        // raw visibilities (TMA destination)
+    L.vexp = off; off += (size_t)tile_vis * 96;        // expanded operand pairs
     L.coef = off; off += (size_t)kMaxTT * 48;          // per timestep: (a,a,b,b) (g,g,qu,qu) (qv,qv,qw,qw)
     L.kappa = off; off += (size_t)C * 8;               // (kappa, kappa)
     off = (off + 15) & ~size_t(15);
@@ -86,10 +82,14 @@ __device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
     s = pack2(s0, s1);
 }
 
-__global__ void __launch_bounds__(kT, 3) gridder_fast_kernel(KernelArgs a) {
+// Kernel shape: NT threads per CTA, PAIRS pixel pairs per thread per pass,
+// TV visibilities per staged tile, at least MINB CTAs per SM (register cap).
+template <int NT, int PAIRS, int TV, int MINB>
+__global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
+    constexpr int kT = NT, kPairs = PAIRS, kPassPairs = NT * PAIRS, kTileVis = TV, kMaxChunk = TV;
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = a.S, S2 = S * S, npairs = S2 / 2;
-    const Layout L = layout(S, a.C);
+    const Layout L = layout(S, a.C, TV);
     SmemHead *head = reinterpret_cast<SmemHead *>(smem);
     float4 *raw = reinterpret_cast<float4 *>(smem + L.raw);
     float4 *vexp = reinterpret_cast<float4 *>(smem + L.vexp);
@@ -318,24 +318,49 @@ __global__ void __launch_bounds__(kT, 3) gridder_fast_kernel(KernelArgs a) {
     }
 }
 
-} // namespace
+// Shapes the autotuner chooses from (index = IDG batched-gridder shape id).
+struct Shape {
+    int nt, pairs, tv, minb;
+};
+constexpr Shape kShapes[] = {
+    {128, 4, 256, 3}, // 12 warps/SM, 8 pixels per thread
+    {128, 2, 128, 4}, // 16 warps/SM, 4 pixels per thread
+    {256, 2, 256, 2}, // 16 warps/SM, 4 pixels per thread, bigger tiles
+    {128, 2, 128, 5}, // 20 warps/SM, register cap ~100
+    {64, 4, 128, 6},  // 12 warps/SM in small CTAs
+};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-size_t gridder_fast_smem(int S, int C) { return layout(S, C).total; }
-
-cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream) {
-    const size_t smem = layout(a.S, a.C).total;
-    cudaError_t e = cudaFuncSetAttribute(gridder_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int NT, int PAIRS, int TV, int MINB>
+cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
+    auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB>;
+    const size_t smem = layout(a.S, a.C, TV).total;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gridder_fast_kernel, kT, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
     if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
-    gridder_fast_kernel<<<(unsigned)blocks, kT, smem, stream>>>(a);
+    kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
     return cudaGetLastError();
+}
+
+} // namespace
+
+int gridder_fast_shapes() { return kNumShapes; }
+
+cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
+    switch (shape) {
+    case 1: return launch_shape<128, 2, 128, 4>(a, stream);
+    case 2: return launch_shape<256, 2, 256, 2>(a, stream);
+    case 3: return launch_shape<128, 2, 128, 5>(a, stream);
+    case 4: return launch_shape<64, 4, 128, 6>(a, stream);
+    default: return launch_shape<128, 4, 256, 3>(a, stream);
+    }
 }
 
 } // namespace idg

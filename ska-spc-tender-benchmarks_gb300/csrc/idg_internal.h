@@ -12,8 +12,16 @@ struct KernelArgs;
 // IDG_VARIANT_BATCHED: persistent packed-FP32x2 kernels (idg_*_fast.cu); need a.work_counter.
 cudaError_t launch_gridder(const KernelArgs &a, int variant, int max_nc, cudaStream_t stream);
 cudaError_t launch_degridder(const KernelArgs &a, int variant, int max_nc, cudaStream_t stream);
-cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream);
-cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream);
+// shape: index into the batched gridder's launch shapes (see gridder_fast_shapes()).
+cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape);
+int gridder_fast_shapes();
+// The shape the batched gridder uses on the current device for subgrid size S.
+int batched_gridder_shape(int S);
+void set_batched_gridder_shape(int S, int shape);
+cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int shape);
+int degridder_fast_shapes();
+int batched_degridder_shape(int S);
+void set_batched_degridder_shape(int S, int shape);
 
 bool fft_size_supported(int S);
 cudaError_t launch_subgrid_fft(float2 *data, int64_t nr_subgrids, int S, int direction, const float *taper,

@@ -110,7 +110,7 @@ extern "C" IDG_API int idg_gridder_noalloc(const idg_params *params, int64_t nr_
     a.subgrids = reinterpret_cast<float2 *>(subgrids);
     a.work_counter = reinterpret_cast<int *>(scratch);
     a.status = reinterpret_cast<unsigned *>(scratch) + 1;
-    cudaError_t e = launch_gridder_fast(a, st);
+    cudaError_t e = launch_gridder_fast(a, st, batched_gridder_shape(a.S));
     if (e != cudaSuccess) return cuda_fail(e, "allocation-free gridder launch");
     return IDG_OK;
 }

@@ -131,6 +131,12 @@ _SIGNATURES = {
                               ctypes.POINTER(IdgBenchmarkResult)],
     "idg_reference_dataset": [_I64, _I64, _I64, _I64, _I64, _I64, ctypes.c_float, _P, _P, _P, _P, _P, _P, _P, _P],
     "idg_measure_fp32_peak": [ctypes.POINTER(ctypes.c_double)],
+    "idg_batched_shapes": [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+    "idg_set_batched_shapes": [_I32, _I32, _I32],
+    "idg_get_batched_shapes": [_I32, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+    "idg_autotune": [ctypes.POINTER(IdgParams), _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I32,
+                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                     ctypes.POINTER(ctypes.c_int)],
 }
 _RESTYPES = {"idg_last_error": ctypes.c_char_p, "idg_abi_version": ctypes.c_int}
 

@@ -273,3 +273,39 @@ def test_large_phase_path(oracle_mod, idg):
     for variant in VARIANTS:
         vgot = degrid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, spec.n_rows, variant)
         check_rel(f"degridder large-phase v{variant}", vgot, vwant, TOL)
+
+
+def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
+    """Each compiled launch shape of the batched kernels gives the same parity; the
+    autotuner times them all and leaves the fastest selected."""
+    from idg_gb300 import tuning
+
+    spec, obs = _config1_obs(aterm_sigma=0.05)
+    vis = _vis(spec, seed=12)
+    S = spec.subgrid_size
+    sp = spec_for(spec.grid_size, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    prm = oracle_mod.params(spec.grid_size, S, spec.nchannels, spec.nstations, spec.n_subgrids, spec.image_size)
+    want = oracle_mod.gridder(prm, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, obs.metadata)
+    rng = np.random.default_rng(13)
+    sub = (rng.standard_normal((spec.n_subgrids, 4, S, S)) + 1j * rng.standard_normal((spec.n_subgrids, 4, S, S))).astype(np.complex64)
+    vwant = oracle_mod.degridder(prm, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, obs.metadata, spec.n_rows)
+    ng, nd = tuning.num_shapes()
+    assert ng >= 2 and nd >= 2
+    for sh in range(max(ng, nd)):
+        tuning.set_shapes(S, min(sh, ng - 1), min(sh, nd - 1))
+        got = grid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, L.VARIANT_BATCHED)
+        check_rel(f"gridder shape {min(sh, ng - 1)}", got, want, TOL)
+        vg = degrid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, spec.n_rows,
+                        L.VARIANT_BATCHED)
+        check_rel(f"degridder shape {min(sh, nd - 1)}", vg, vwant, TOL)
+    # autotuner on device data
+    d = {k: dev(v) for k, v in dict(md=obs.metadata, uvw=obs.uvw, k=obs.wavenumbers, vis=vis, taper=obs.taper,
+                                    at=obs.aterms).items()}
+    out_sub = torch.empty((spec.n_subgrids, 4, S, S), dtype=torch.complex64, device="cuda")
+    out_vis = torch.empty_like(d["vis"])
+    res = tuning.autotune(sp, d["md"], d["uvw"], d["k"], d["vis"], d["taper"], d["at"], out_sub, out_vis, repeats=1,
+                          store=False)
+    assert len(res["gridder_ms"]) == ng and all(t > 0 for t in res["gridder_ms"])
+    assert tuning.get_shapes(S) == (res["gridder"], res["degridder"])
+    assert res["gridder_ms"][res["gridder"]] == min(res["gridder_ms"])
+    tuning.set_shapes(S, 0, 0)
