@@ -188,6 +188,106 @@ IDG_API int idg_degrid_visibilities(const idg_params *params, int variant, int64
                                     const float *spheroidal, const void *aterms, void *subgrids, const void *grid,
                                     void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Execution plans (batching form): device-resident plan + CUDA graph  */
+/* ------------------------------------------------------------------ */
+/* A plan keeps a set of subgrids on the device: metadata, channel sidecar, a
+ * work list ordering the subgrids longest first (uneven subgrids then finish
+ * together in one persistent launch), the plan's own scheduler words and the
+ * subgrid work space.  `metadata` and `ext` are HOST arrays, validated and
+ * copied at creation.  The steps are those of idg_grid_visibilities /
+ * idg_degrid_visibilities.  No counterpart in the reference. */
+typedef struct idg_plan idg_plan;
+IDG_API int idg_plan_create(const idg_params *params, int variant, int64_t nr_subgrids, const idg_metadata *metadata,
+                            const idg_subgrid_ext *ext, int64_t nr_rows, idg_plan **plan);
+IDG_API int idg_plan_destroy(idg_plan *plan);
+/* Caps the persistent kernels of this plan at max_ctas CTAs (0 = fill the GPU),
+ * so that several plans can share the GPU at the same time. */
+IDG_API int idg_plan_set_cta_limit(idg_plan *plan, int max_ctas);
+IDG_API int idg_plan_grid(idg_plan *plan, const float *uvw, const float *wavenumbers, const void *visibilities,
+                          const float *spheroidal, const void *aterms, void *grid, void *stream);
+IDG_API int idg_plan_degrid(idg_plan *plan, const float *uvw, const float *wavenumbers, void *visibilities,
+                            const float *spheroidal, const void *aterms, const void *grid, void *stream);
+/* Captures one imaging cycle on these device buffers -- zero `grid`, grid
+ * `visibilities_in` into it, degrid it into `visibilities_out` -- as a CUDA
+ * graph; idg_plan_launch_cycle() replays it with a single launch. */
+IDG_API int idg_plan_capture_cycle(idg_plan *plan, const float *uvw, const float *wavenumbers,
+                                   const void *visibilities_in, const float *spheroidal, const void *aterms, void *grid,
+                                   void *visibilities_out);
+IDG_API int idg_plan_launch_cycle(idg_plan *plan, void *stream);
+/* Reads (and optionally clears) the plan's device check word; synchronises `stream`. */
+IDG_API int idg_plan_status(idg_plan *plan, void *stream, uint32_t *status, int clear);
+
+/* ------------------------------------------------------------------ */
+/* Serving: continuous batching of gridding / degridding jobs          */
+/* ------------------------------------------------------------------ */
+/* A server runs a scheduler thread that admits submitted jobs, in arrival
+ * order, whenever one of `max_slots` slots (CUDA streams) is free and the
+ * job's device footprint fits what `hbm_budget_bytes` leaves after the running
+ * jobs (a job that cannot fit at all is rejected at submission; a job that
+ * does not fit yet is overtaken by later jobs on other grids).  Admitted jobs
+ * run concurrently: copies in, the batched kernels, copies out, each on its
+ * slot's stream; with `cta_share` the persistent kernels of concurrently
+ * running jobs split the SMs.  uv-grids are device-resident and owned by the
+ * server; gridding jobs add into one, degridding jobs read one, and jobs of a
+ * different kind on the same grid are ordered on the GPU.  Host buffers of a
+ * job must stay valid until idg_server_wait() returns for it and should be
+ * pinned (page-locked) for full copy bandwidth; every submitted job must be
+ * waited on.  No counterpart in the reference. */
+typedef struct idg_server idg_server;
+typedef struct idg_server_config {
+    int32_t max_slots;        /* jobs on the GPU at once (1..64) */
+    int32_t cta_share;        /* nonzero: running jobs share the SMs between their persistent kernels */
+    int64_t hbm_budget_bytes; /* device memory jobs may hold at once (resident grids not counted) */
+} idg_server_config;
+
+#define IDG_JOB_GRID 0
+#define IDG_JOB_DEGRID 1
+typedef struct idg_job {
+    int32_t op;      /* IDG_JOB_GRID or IDG_JOB_DEGRID */
+    int32_t variant; /* IDG_VARIANT_* */
+    idg_params params;
+    int64_t nr_subgrids;
+    const idg_metadata *metadata; /* host */
+    const idg_subgrid_ext *ext;   /* host, may be NULL */
+    int64_t nr_rows;
+    const float *uvw;         /* host [nr_rows][3] */
+    const float *wavenumbers; /* host [C] */
+    const void *vis_in;       /* host [nr_rows][C][4] complex64 (gridding jobs) */
+    void *vis_out;            /* host [nr_rows][C][4] complex64 (degridding jobs) */
+    const float *spheroidal;  /* host [S][S] */
+    const void *aterms;       /* host [nr_aterms][stations][S][S][4] complex64 */
+    int64_t grid_id;          /* a grid from idg_server_grid_create */
+} idg_job;
+
+typedef struct idg_job_stats {
+    double queue_ms;   /* submission to admission */
+    double run_ms;     /* admission to completion */
+    double latency_ms; /* submission to completion */
+    int64_t visibilities;
+    int32_t status;
+    int32_t reserved;
+} idg_job_stats;
+
+typedef struct idg_server_stats {
+    int64_t completed, rejected, failed, queued, running;
+    int64_t hbm_in_use, hbm_peak;
+    double p50_ms, p99_ms, mean_ms; /* job latency (submission to completion) over completed jobs */
+    double mvis_per_s;              /* visibilities of completed jobs / (first submission .. last completion) */
+} idg_server_summary;
+
+IDG_API int idg_server_create(const idg_server_config *config, idg_server **server);
+/* Finishes the queued and running jobs, then frees everything. */
+IDG_API int idg_server_destroy(idg_server *server);
+IDG_API int idg_server_grid_create(idg_server *server, int32_t grid_size, int32_t nr_w_planes, int64_t *grid_id);
+/* Copies a grid to the host after the jobs running on it. */
+IDG_API int idg_server_grid_read(idg_server *server, int64_t grid_id, void *host_out);
+IDG_API int idg_server_grid_release(idg_server *server, int64_t grid_id);
+IDG_API int idg_server_submit(idg_server *server, const idg_job *job, int64_t *job_id);
+/* Waits at most timeout_ms for a job (IDG_ERR_TIMEOUT otherwise); returns the job's status. */
+IDG_API int idg_server_wait(idg_server *server, int64_t job_id, int64_t timeout_ms, idg_job_stats *stats);
+IDG_API int idg_server_stats(idg_server *server, idg_server_summary *stats);
+
 /* Timing of one host-buffer imaging cycle (milliseconds, bytes). */
 typedef struct idg_cycle_timing {
     double total_ms;      /* first host-to-device copy issued .. last device-to-host copy done */

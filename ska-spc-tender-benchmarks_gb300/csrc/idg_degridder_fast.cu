@@ -290,6 +290,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (a.max_ctas > 0 && blocks > a.max_ctas) blocks = a.max_ctas;
     if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
     kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
     return cudaGetLastError();
@@ -298,13 +299,14 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 } // namespace
 
 // Launch shapes of the batched degridder (index = shape id).
-int degridder_fast_shapes() { return 4; }
+int degridder_fast_shapes() { return 5; }
 
 cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
     case 1: return launch_shape<128, 512, 4>(a, stream); // 16 warps/SM, register cap 128
     case 2: return launch_shape<256, 512, 2>(a, stream); // 16 warps/SM in 256-thread CTAs
     case 3: return launch_shape<128, 256, 4>(a, stream); // smaller staging batches
+    case 4: return launch_shape<128, 512, 2>(a, stream); // 8 warps/SM, registers uncapped
     default: return launch_shape<128, 512, 3>(a, stream); // 12 warps/SM
     }
 }

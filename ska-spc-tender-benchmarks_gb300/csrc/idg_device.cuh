@@ -118,6 +118,7 @@ struct KernelArgs {
     const int *work_list; // batched variant: subgrid order (may be NULL)
     int *work_counter;    // batched variant: dynamic scheduler (may be NULL)
     unsigned *status;     // device check word (may be NULL)
+    int max_ctas;         // persistent kernels: at most this many CTAs (0 = fill the GPU)
 };
 
 // Plan entry after validation.

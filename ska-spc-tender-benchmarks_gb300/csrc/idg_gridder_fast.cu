@@ -82,9 +82,90 @@ __device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
     s = pack2(s0, s1);
 }
 
+// Phasors of one channel for all pixel pairs of the thread.
+template <int PAIRS, bool FAST>
+__device__ __forceinline__ void channel_phasors(f2 kc, const f2 (&tau0)[PAIRS], const f2 (&Q)[PAIRS], f2 (&C)[PAIRS],
+                                                f2 (&Sn)[PAIRS]) {
+#pragma unroll
+    for (int j = 0; j < PAIRS; ++j) {
+        f2 x = ffma2(kc, Q[j], tau0[j]);
+        if (!FAST) x = reduce_2pi(x);
+        sincos_pair(x, C[j], Sn[j]);
+    }
+}
+
+// P += V * (cos + i sin) for every pixel pair: re += vr c - vi s ; im += vr s + vi c
+template <int PAIRS>
+__device__ __forceinline__ void channel_macs(f2 (&acc)[PAIRS][8], const float4 *vv, const f2 (&C)[PAIRS],
+                                             const f2 (&Sn)[PAIRS]) {
+    const float4 e0 = vv[0], e1 = vv[1], e2 = vv[2], e3 = vv[3], e4 = vv[4], e5 = vv[5];
+    const f2 vr0 = pack2(e0.x, e0.y), vi0 = pack2(e0.z, e0.w);
+    const f2 vr1 = pack2(e1.x, e1.y), vi1 = pack2(e1.z, e1.w);
+    const f2 vr2 = pack2(e2.x, e2.y), vi2 = pack2(e2.z, e2.w);
+    const f2 vr3 = pack2(e3.x, e3.y), vi3 = pack2(e3.z, e3.w);
+    const f2 ni0 = pack2(e4.x, e4.y), ni1 = pack2(e4.z, e4.w);
+    const f2 ni2 = pack2(e5.x, e5.y), ni3 = pack2(e5.z, e5.w);
+#pragma unroll
+    for (int j = 0; j < PAIRS; ++j) {
+        acc[j][0] = ffma2(ni0, Sn[j], ffma2(vr0, C[j], acc[j][0]));
+        acc[j][1] = ffma2(vi0, C[j], ffma2(vr0, Sn[j], acc[j][1]));
+        acc[j][2] = ffma2(ni1, Sn[j], ffma2(vr1, C[j], acc[j][2]));
+        acc[j][3] = ffma2(vi1, C[j], ffma2(vr1, Sn[j], acc[j][3]));
+        acc[j][4] = ffma2(ni2, Sn[j], ffma2(vr2, C[j], acc[j][4]));
+        acc[j][5] = ffma2(vi2, C[j], ffma2(vr2, Sn[j], acc[j][5]));
+        acc[j][6] = ffma2(ni3, Sn[j], ffma2(vr3, C[j], acc[j][6]));
+        acc[j][7] = ffma2(vi3, C[j], ffma2(vr3, Sn[j], acc[j][7]));
+    }
+}
+
+// One staged tile: tt timesteps x ncc channels.
+// PIPE = 1: the channel loop is software pipelined -- the sincos of channel c+1
+// is issued before the MACs of channel c, so a warp keeps SFU and FMA work in
+// flight together (more registers).  PIPE = 0: phasors then MACs per channel.
+template <int PAIRS, bool FAST, int PIPE>
+__device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[PAIRS], const float4 *coef,
+                                          const f2 *geo, const float4 *vexp, const f2 *kp, int tt, int ncc) {
+    for (int t = 0; t < tt; ++t) {
+        const float4 c0 = coef[3 * t], c1 = coef[3 * t + 1], c2 = coef[3 * t + 2];
+        const f2 A2 = pack2(c0.x, c0.y), B2 = pack2(c0.z, c0.w), G2 = pack2(c1.x, c1.y);
+        const f2 QU = pack2(c1.z, c1.w), QV = pack2(c2.x, c2.y), QW = pack2(c2.z, c2.w);
+        f2 tau0[PAIRS], Q[PAIRS];
+#pragma unroll
+        for (int j = 0; j < PAIRS; ++j) {
+            const f2 hx = geo[3 * pr[j]], hy = geo[3 * pr[j] + 1], nn = geo[3 * pr[j] + 2];
+            tau0[j] = reduce_2pi(ffma2(A2, hx, ffma2(B2, hy, fmul2(G2, nn))));
+            Q[j] = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
+        }
+        const float4 *vt = vexp + (size_t)t * ncc * 6;
+        if (PIPE) {
+            f2 Cn[PAIRS], Sn[PAIRS];
+            channel_phasors<PAIRS, FAST>(kp[0], tau0, Q, Cn, Sn);
+#pragma unroll 1
+            for (int c = 0; c + 1 < ncc; ++c) {
+                f2 C[PAIRS], S[PAIRS];
+#pragma unroll
+                for (int j = 0; j < PAIRS; ++j) {
+                    C[j] = Cn[j];
+                    S[j] = Sn[j];
+                }
+                channel_phasors<PAIRS, FAST>(kp[c + 1], tau0, Q, Cn, Sn);
+                channel_macs<PAIRS>(acc, vt + 6 * c, C, S);
+            }
+            channel_macs<PAIRS>(acc, vt + 6 * (ncc - 1), Cn, Sn);
+        } else {
+#pragma unroll 1
+            for (int c = 0; c < ncc; ++c) {
+                f2 C[PAIRS], S[PAIRS];
+                channel_phasors<PAIRS, FAST>(kp[c], tau0, Q, C, S);
+                channel_macs<PAIRS>(acc, vt + 6 * c, C, S);
+            }
+        }
+    }
+}
+
 // Kernel shape: NT threads per CTA, PAIRS pixel pairs per thread per pass,
 // TV visibilities per staged tile, at least MINB CTAs per SM (register cap).
-template <int NT, int PAIRS, int TV, int MINB>
+template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
     constexpr int kT = NT, kPairs = PAIRS, kPassPairs = NT * PAIRS, kTileVis = TV, kMaxChunk = TV;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -227,48 +308,10 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
                     const bool fast = head->fast != 0;
 
                     // ---- compute
-                    for (int t = 0; t < tt; ++t) {
-                        const float4 c0 = coef[3 * t], c1 = coef[3 * t + 1], c2 = coef[3 * t + 2];
-                        const f2 A2 = pack2(c0.x, c0.y), B2 = pack2(c0.z, c0.w), G2 = pack2(c1.x, c1.y);
-                        const f2 QU = pack2(c1.z, c1.w), QV = pack2(c2.x, c2.y), QW = pack2(c2.z, c2.w);
-                        f2 tau0[kPairs], Q[kPairs];
-#pragma unroll
-                        for (int j = 0; j < kPairs; ++j) {
-                            const f2 hx = geo[3 * pr[j]], hy = geo[3 * pr[j] + 1], nn = geo[3 * pr[j] + 2];
-                            tau0[j] = reduce_2pi(ffma2(A2, hx, ffma2(B2, hy, fmul2(G2, nn))));
-                            Q[j] = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
-                        }
-                        const float4 *vt = vexp + (size_t)t * ncc * 6;
-                        const f2 *kp = kap + cb;
-#pragma unroll 1
-                        for (int c = 0; c < ncc; ++c) {
-                            const f2 kc = kp[c];
-                            const float4 *vv = vt + 6 * c;
-                            const float4 e0 = vv[0], e1 = vv[1], e2 = vv[2], e3 = vv[3], e4 = vv[4], e5 = vv[5];
-                            const f2 vr0 = pack2(e0.x, e0.y), vi0 = pack2(e0.z, e0.w);
-                            const f2 vr1 = pack2(e1.x, e1.y), vi1 = pack2(e1.z, e1.w);
-                            const f2 vr2 = pack2(e2.x, e2.y), vi2 = pack2(e2.z, e2.w);
-                            const f2 vr3 = pack2(e3.x, e3.y), vi3 = pack2(e3.z, e3.w);
-                            const f2 ni0 = pack2(e4.x, e4.y), ni1 = pack2(e4.z, e4.w);
-                            const f2 ni2 = pack2(e5.x, e5.y), ni3 = pack2(e5.z, e5.w);
-#pragma unroll
-                            for (int j = 0; j < kPairs; ++j) {
-                                f2 x = ffma2(kc, Q[j], tau0[j]);
-                                if (!fast) x = reduce_2pi(x);
-                                f2 C, Sn;
-                                sincos_pair(x, C, Sn);
-                                // P += V * (cos + i sin): re += vr c - vi s ; im += vr s + vi c
-                                acc[j][0] = ffma2(ni0, Sn, ffma2(vr0, C, acc[j][0]));
-                                acc[j][1] = ffma2(vi0, C, ffma2(vr0, Sn, acc[j][1]));
-                                acc[j][2] = ffma2(ni1, Sn, ffma2(vr1, C, acc[j][2]));
-                                acc[j][3] = ffma2(vi1, C, ffma2(vr1, Sn, acc[j][3]));
-                                acc[j][4] = ffma2(ni2, Sn, ffma2(vr2, C, acc[j][4]));
-                                acc[j][5] = ffma2(vi2, C, ffma2(vr2, Sn, acc[j][5]));
-                                acc[j][6] = ffma2(ni3, Sn, ffma2(vr3, C, acc[j][6]));
-                                acc[j][7] = ffma2(vi3, C, ffma2(vr3, Sn, acc[j][7]));
-                            }
-                        }
-                    }
+                    if (fast)
+                        grid_tile<kPairs, true, PIPE>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
+                    else
+                        grid_tile<kPairs, false, PIPE>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
                 }
                 if (head->abort) break;
             }
@@ -318,22 +361,15 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
     }
 }
 
-// Shapes the autotuner chooses from (index = IDG batched-gridder shape id).
-struct Shape {
-    int nt, pairs, tv, minb;
-};
-constexpr Shape kShapes[] = {
-    {128, 4, 256, 3}, // 12 warps/SM, 8 pixels per thread
-    {128, 2, 128, 4}, // 16 warps/SM, 4 pixels per thread
-    {256, 2, 256, 2}, // 16 warps/SM, 4 pixels per thread, bigger tiles
-    {128, 2, 128, 5}, // 20 warps/SM, register cap ~100
-    {64, 4, 128, 6},  // 12 warps/SM in small CTAs
-};
-constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
-
-template <int NT, int PAIRS, int TV, int MINB>
+// Launch shapes the autotuner chooses from (index = batched-gridder shape id):
+//   0: 128 threads x 4 pairs, 256-visibility tiles, 3 CTAs/SM (12 warps), plain channel loop
+//   1: 128 x 4, 2 CTAs/SM (8 warps), software-pipelined channel loop, registers uncapped
+//   2: 128 x 2, 128-visibility tiles, 4 CTAs/SM (16 warps), pipelined
+//   3: 256 x 2, 256-visibility tiles, 2 CTAs/SM (16 warps), pipelined
+//   4: 128 x 2, 128-visibility tiles, 4 CTAs/SM (16 warps), plain channel loop
+template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
-    auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB>;
+    auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
     const size_t smem = layout(a.S, a.C, TV).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -344,6 +380,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (a.max_ctas > 0 && blocks > a.max_ctas) blocks = a.max_ctas;
     if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
     kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
     return cudaGetLastError();
@@ -351,15 +388,15 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return kNumShapes; }
+int gridder_fast_shapes() { return 5; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
-    case 1: return launch_shape<128, 2, 128, 4>(a, stream);
-    case 2: return launch_shape<256, 2, 256, 2>(a, stream);
-    case 3: return launch_shape<128, 2, 128, 5>(a, stream);
-    case 4: return launch_shape<64, 4, 128, 6>(a, stream);
-    default: return launch_shape<128, 4, 256, 3>(a, stream);
+    case 1: return launch_shape<128, 4, 256, 2, 1>(a, stream);
+    case 2: return launch_shape<128, 2, 128, 4, 1>(a, stream);
+    case 3: return launch_shape<256, 2, 256, 2, 1>(a, stream);
+    case 4: return launch_shape<128, 2, 128, 4, 0>(a, stream);
+    default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }
 

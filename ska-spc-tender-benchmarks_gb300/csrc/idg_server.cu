@@ -1,0 +1,512 @@
+// idg_server.cu -- the serving loop: continuous batching of gridding and
+// degridding jobs on one GPU.
+//
+// Jobs arrive on any thread through idg_server_submit().  A scheduler thread
+// admits them in arrival order whenever a slot (a CUDA stream) is free and the
+// job's device footprint fits the HBM budget left by the jobs already running
+// -- a job that can never fit is rejected at submission.  An admitted job gets
+// one stream-ordered allocation for its plan, subgrid work space and data, its
+// copies in, the batched kernels of its step and its copies out, all on its
+// slot's stream; so jobs that are admitted while others run overlap on the
+// device (copies against kernels, and kernels against kernels when the
+// persistent kernels' CTA budget is shared between the running jobs).  uv-grids
+// live on the device for the server's lifetime: gridding jobs add into one,
+// degridding jobs read one; a job whose kind differs from the running jobs on
+// the same grid waits for them on the GPU (stream-ordered event waits).  The
+// scheduler polls completion events (never blocks in a CUDA call), records
+// queueing, run and total latency per job, and frees the job's memory.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+#include "idg_device.cuh"
+#include "idg_host.h"
+#include "idg_internal.h"
+
+using namespace idg;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct Grid {
+    void *dev = nullptr;
+    size_t bytes = 0;
+    int32_t size = 0, planes = 1;
+    int last_op = -1;                  // op of the jobs currently holding the grid
+    std::vector<cudaEvent_t> holders;  // their completion events
+};
+
+struct Job {
+    int64_t id = 0;
+    idg_job spec{};
+    std::vector<idg_metadata> md;
+    std::vector<idg_subgrid_ext> ext;
+    std::vector<int> work;
+    size_t footprint = 0;
+    int64_t nvis = 0;
+    Clock::time_point t_submit, t_admit, t_done;
+    int slot = -1;
+    void *arena = nullptr;
+    cudaEvent_t done = nullptr;
+    int status = IDG_OK;
+    bool finished = false;
+};
+
+size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Layout {
+    size_t md, ext, work, words, sub, uvw, k, taper, aterms, vis, total;
+};
+
+Layout job_layout(const idg_job &j) {
+    const idg_params &p = j.params;
+    const size_t N = (size_t)j.nr_subgrids, S = (size_t)p.subgrid_size;
+    Layout L;
+    size_t off = 0;
+    L.md = off; off += align_up(sizeof(idg_metadata) * N);
+    L.ext = off; off += j.ext ? align_up(sizeof(idg_subgrid_ext) * N) : 0;
+    L.work = off; off += align_up(sizeof(int) * N);
+    L.words = off; off += 256;
+    L.sub = off; off += align_up(N * 4 * S * S * 8);
+    L.uvw = off; off += align_up((size_t)j.nr_rows * 12);
+    L.k = off; off += align_up((size_t)p.nr_channels * 4);
+    L.taper = off; off += align_up(S * S * 4);
+    L.aterms = off; off += align_up((size_t)p.nr_aterms * p.nr_stations * S * S * 32);
+    L.vis = off; off += align_up((size_t)j.nr_rows * p.nr_channels * 32);
+    L.total = off;
+    return L;
+}
+
+} // namespace
+
+struct idg_server {
+    idg_server_config cfg{};
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Job>> queue;
+    std::map<int64_t, std::shared_ptr<Job>> jobs;
+    std::vector<std::shared_ptr<Job>> slots;
+    std::vector<cudaStream_t> streams;
+    std::map<int64_t, Grid> grids;
+    int64_t next_job = 1, next_grid = 1;
+    size_t in_use = 0, peak_use = 0;
+    int64_t completed = 0, rejected = 0, failed = 0, total_vis = 0;
+    std::vector<double> latencies;
+    Clock::time_point first_submit{}, last_done{};
+    bool have_first = false;
+    bool stop = false;
+    int full_ctas = 0; // CTAs a persistent kernel uses when it fills the GPU
+    std::thread worker;
+
+    void run();
+    void admit_locked();
+    void launch(Job &j);
+    void poll_locked();
+};
+
+namespace {
+
+int validate_job(const idg_server *srv, const idg_job *j) {
+    if (!j) return fail(IDG_ERR_INVALID_ARGUMENT, "job is NULL");
+    if (j->op != IDG_JOB_GRID && j->op != IDG_JOB_DEGRID) return fail(IDG_ERR_INVALID_ARGUMENT, "unknown job op %d", j->op);
+    if (int rc = check_params(&j->params, true)) return rc;
+    if (j->nr_subgrids < 1 || j->nr_subgrids > INT32_MAX) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_subgrids");
+    if (j->nr_rows < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_rows");
+    if (!j->metadata || !j->uvw || !j->wavenumbers || !j->spheroidal || !j->aterms)
+        return fail(IDG_ERR_INVALID_ARGUMENT, "NULL host array");
+    if (j->op == IDG_JOB_GRID && !j->vis_in) return fail(IDG_ERR_INVALID_ARGUMENT, "gridding job without vis_in");
+    if (j->op == IDG_JOB_DEGRID && !j->vis_out) return fail(IDG_ERR_INVALID_ARGUMENT, "degridding job without vis_out");
+    auto it = srv->grids.find(j->grid_id);
+    if (it == srv->grids.end()) return fail(IDG_ERR_NOT_FOUND, "unknown grid %lld", (long long)j->grid_id);
+    if (it->second.size != j->params.grid_size || it->second.planes != (j->params.nr_w_planes > 0 ? j->params.nr_w_planes : 1))
+        return fail(IDG_ERR_INVALID_ARGUMENT, "job geometry does not match grid %lld", (long long)j->grid_id);
+    const int bo1 = j->metadata[0].baseline_offset;
+    for (int64_t s = 0; s < j->nr_subgrids; ++s) {
+        const idg_metadata &m = j->metadata[s];
+        const int64_t r0 = (int64_t)(m.baseline_offset - bo1) + m.time_offset;
+        int c0 = 0, c1 = j->params.nr_channels;
+        if (j->ext) {
+            c0 = j->ext[s].channel_begin;
+            c1 = j->ext[s].channel_end;
+        }
+        if (r0 < 0 || m.nr_timesteps < 0 || r0 + m.nr_timesteps > j->nr_rows ||
+            m.station1 >= (uint32_t)j->params.nr_stations || m.station2 >= (uint32_t)j->params.nr_stations ||
+            m.aterm_index < 0 || m.aterm_index >= j->params.nr_aterms || c0 < 0 || c1 > j->params.nr_channels || c0 > c1)
+            return fail(IDG_ERR_INVALID_ARGUMENT, "job plan entry %lld is out of range", (long long)s);
+    }
+    return IDG_OK;
+}
+
+} // namespace
+
+void idg_server::launch(Job &j) {
+    cudaSetDevice(device);
+    cudaStream_t st = streams[j.slot];
+    const idg_params &p = j.spec.params;
+    const Layout L = job_layout(j.spec);
+    char *base = static_cast<char *>(j.arena);
+    auto dp = [&](size_t off) { return static_cast<void *>(base + off); };
+    const size_t N = j.md.size();
+    const int64_t S = p.subgrid_size;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess && x != cudaSuccess) e = x;
+    };
+    chk(cudaMemcpyAsync(dp(L.md), j.md.data(), sizeof(idg_metadata) * N, cudaMemcpyHostToDevice, st));
+    if (!j.ext.empty()) chk(cudaMemcpyAsync(dp(L.ext), j.ext.data(), sizeof(idg_subgrid_ext) * N, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(dp(L.work), j.work.data(), sizeof(int) * N, cudaMemcpyHostToDevice, st));
+    chk(cudaMemsetAsync(dp(L.words), 0, 256, st));
+    chk(cudaMemcpyAsync(dp(L.uvw), j.spec.uvw, (size_t)j.spec.nr_rows * 12, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(dp(L.k), j.spec.wavenumbers, (size_t)p.nr_channels * 4, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(dp(L.taper), j.spec.spheroidal, (size_t)S * S * 4, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(dp(L.aterms), j.spec.aterms, (size_t)p.nr_aterms * p.nr_stations * S * S * 32,
+                        cudaMemcpyHostToDevice, st));
+    const size_t b_vis = (size_t)j.spec.nr_rows * p.nr_channels * 32;
+    if (j.spec.op == IDG_JOB_GRID)
+        chk(cudaMemcpyAsync(dp(L.vis), j.spec.vis_in, b_vis, cudaMemcpyHostToDevice, st));
+    else
+        chk(cudaMemsetAsync(dp(L.vis), 0, b_vis, st));
+
+    Grid &g = grids[j.spec.grid_id];
+    KernelArgs a{};
+    a.G = p.grid_size;
+    a.S = p.subgrid_size;
+    a.C = p.nr_channels;
+    a.nr_stations = p.nr_stations;
+    a.nr_aterms = p.nr_aterms;
+    a.nr_w_planes = g.planes;
+    a.image_size = p.image_size;
+    a.w_step = p.w_step;
+    a.flags = p.flags | IDG_FLAG_NO_TAPER;
+    a.nr_subgrids = (int64_t)N;
+    a.nr_rows = j.spec.nr_rows;
+    a.md = static_cast<const idg_metadata *>(dp(L.md));
+    a.ext = j.ext.empty() ? nullptr : static_cast<const idg_subgrid_ext *>(dp(L.ext));
+    a.uvw = static_cast<const float *>(dp(L.uvw));
+    a.wavenumbers = static_cast<const float *>(dp(L.k));
+    a.taper = static_cast<const float *>(dp(L.taper));
+    a.aterms = static_cast<const float4 *>(dp(L.aterms));
+    a.vis = static_cast<float4 *>(dp(L.vis));
+    a.subgrids = static_cast<float2 *>(dp(L.sub));
+    a.work_list = static_cast<const int *>(dp(L.work));
+    a.work_counter = static_cast<int *>(dp(L.words));
+    a.status = static_cast<unsigned *>(dp(L.words)) + 2;
+    int running = 0;
+    for (auto &s : slots)
+        if (s) ++running;
+    a.max_ctas = (cfg.cta_share && running > 1 && full_ctas > 0) ? std::max(1, full_ctas / running) : 0;
+    const int variant = j.spec.variant == IDG_VARIANT_PLAIN ? IDG_VARIANT_PLAIN : IDG_VARIANT_BATCHED;
+
+    // order against the other jobs on this grid
+    if (g.last_op != -1 && g.last_op != j.spec.op)
+        for (cudaEvent_t h : g.holders) chk(cudaStreamWaitEvent(st, h, 0));
+
+    if (j.spec.op == IDG_JOB_GRID) {
+        chk(launch_gridder(a, variant, p.nr_channels, st));
+        chk(launch_subgrid_fft(a.subgrids, (int64_t)N, p.subgrid_size, +1, a.taper, st));
+        chk(launch_adder(a.md, (int64_t)N, p.subgrid_size, p.grid_size, g.planes, a.subgrids,
+                         static_cast<float2 *>(g.dev), st));
+    } else {
+        chk(launch_splitter(a.md, (int64_t)N, p.subgrid_size, p.grid_size, g.planes,
+                            static_cast<const float2 *>(g.dev), a.subgrids, st));
+        chk(launch_subgrid_fft(a.subgrids, (int64_t)N, p.subgrid_size, -1, a.taper, st));
+        chk(launch_degridder(a, variant, p.nr_channels, st));
+        chk(cudaMemcpyAsync(j.spec.vis_out, dp(L.vis), b_vis, cudaMemcpyDeviceToHost, st));
+    }
+    chk(cudaEventRecord(j.done, st));
+    if (g.last_op != j.spec.op) g.holders.clear();
+    g.last_op = j.spec.op;
+    g.holders.push_back(j.done);
+    if (e != cudaSuccess) j.status = cuda_fail(e, "server job launch");
+}
+
+void idg_server::admit_locked() {
+    // grids with a job left waiting in this scan: later jobs on them must not overtake it
+    std::vector<int64_t> blocked;
+    auto is_blocked = [&](int64_t g) { return std::find(blocked.begin(), blocked.end(), g) != blocked.end(); };
+    for (auto it = queue.begin(); it != queue.end();) {
+        int free_slot = -1;
+        for (int s = 0; s < (int)slots.size(); ++s)
+            if (!slots[s]) {
+                free_slot = s;
+                break;
+            }
+        if (free_slot < 0) return;
+        Job &j = **it;
+        if (is_blocked(j.spec.grid_id) || in_use + j.footprint > (size_t)cfg.hbm_budget_bytes) {
+            blocked.push_back(j.spec.grid_id);
+            ++it; // a smaller job behind it, on another grid, may fit now
+            continue;
+        }
+        cudaSetDevice(device);
+        void *arena = nullptr;
+        cudaError_t e = cudaMallocAsync(&arena, j.footprint, streams[free_slot]);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            blocked.push_back(j.spec.grid_id);
+            ++it; // the pool cannot serve it right now; retry when memory frees up
+            continue;
+        }
+        j.arena = arena;
+        j.slot = free_slot;
+        j.t_admit = Clock::now();
+        slots[free_slot] = *it;
+        in_use += j.footprint;
+        peak_use = std::max(peak_use, in_use);
+        cudaEventCreateWithFlags(&j.done, cudaEventDisableTiming);
+        launch(j);
+        it = queue.erase(it);
+    }
+}
+
+void idg_server::poll_locked() {
+    for (int s = 0; s < (int)slots.size(); ++s) {
+        auto &jp = slots[s];
+        if (!jp) continue;
+        cudaError_t q = jp->status == IDG_OK ? cudaEventQuery(jp->done) : cudaSuccess;
+        if (q == cudaErrorNotReady) continue;
+        Job &j = *jp;
+        j.t_done = Clock::now();
+        if (q != cudaSuccess && j.status == IDG_OK) j.status = cuda_fail(q, "server job");
+        // plan entries the kernels rejected
+        if (j.status == IDG_OK) {
+            unsigned st = 0;
+            const Layout L = job_layout(j.spec);
+            cudaMemcpy(&st, static_cast<char *>(j.arena) + L.words + 8, sizeof st, cudaMemcpyDeviceToHost);
+            if (st) j.status = IDG_ERR_DEVICE_CHECK;
+        }
+        Grid &g = grids[j.spec.grid_id];
+        g.holders.erase(std::remove(g.holders.begin(), g.holders.end(), j.done), g.holders.end());
+        if (g.holders.empty()) g.last_op = -1;
+        cudaFreeAsync(j.arena, streams[s]);
+        cudaEventDestroy(j.done);
+        j.done = nullptr;
+        j.arena = nullptr;
+        in_use -= j.footprint;
+        j.finished = true;
+        if (j.status == IDG_OK) {
+            ++completed;
+            total_vis += j.nvis;
+            latencies.push_back(ms_between(j.t_submit, j.t_done));
+            last_done = j.t_done;
+        } else {
+            ++failed;
+        }
+        jp.reset();
+        cv_done.notify_all();
+    }
+}
+
+void idg_server::run() {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lock(mu);
+    for (;;) {
+        poll_locked();
+        admit_locked();
+        bool running = false;
+        for (auto &s : slots)
+            if (s) running = true;
+        if (stop && !running && queue.empty()) break;
+        // short sleep while kernels run; wake at once on new work
+        cv_work.wait_for(lock, std::chrono::microseconds(running ? 100 : 2000));
+    }
+}
+
+extern "C" {
+
+IDG_API int idg_server_create(const idg_server_config *cfg, idg_server **out) {
+    if (!cfg || !out) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (cfg->max_slots < 1 || cfg->max_slots > 64) return fail(IDG_ERR_INVALID_ARGUMENT, "max_slots %d", cfg->max_slots);
+    if (cfg->hbm_budget_bytes < (1 << 20)) return fail(IDG_ERR_INVALID_ARGUMENT, "hbm budget too small");
+    auto *srv = new idg_server;
+    srv->cfg = *cfg;
+    cudaGetDevice(&srv->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, srv->device);
+    srv->full_ctas = sms * 3;
+    srv->slots.resize(cfg->max_slots);
+    srv->streams.resize(cfg->max_slots);
+    for (auto &s : srv->streams) {
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            for (auto &t : srv->streams)
+                if (t) cudaStreamDestroy(t);
+            delete srv;
+            return cuda_fail(e, "server stream");
+        }
+    }
+    // keep freed job memory in the pool between jobs
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, srv->device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    srv->worker = std::thread([srv] { srv->run(); });
+    *out = srv;
+    return IDG_OK;
+}
+
+IDG_API int idg_server_destroy(idg_server *srv) {
+    if (!srv) return IDG_OK;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        srv->stop = true;
+    }
+    srv->cv_work.notify_all();
+    srv->worker.join();
+    cudaSetDevice(srv->device);
+    for (auto &g : srv->grids) cudaFree(g.second.dev);
+    for (auto &s : srv->streams) cudaStreamDestroy(s);
+    delete srv;
+    return IDG_OK;
+}
+
+IDG_API int idg_server_grid_create(idg_server *srv, int32_t grid_size, int32_t nr_w_planes, int64_t *grid_id) {
+    if (!srv || !grid_id) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (grid_size < 1 || nr_w_planes < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "bad grid size");
+    Grid g;
+    g.size = grid_size;
+    g.planes = nr_w_planes;
+    g.bytes = (size_t)nr_w_planes * 4 * grid_size * grid_size * 8;
+    cudaSetDevice(srv->device);
+    IDG_CUDA(cudaMalloc(&g.dev, g.bytes));
+    IDG_CUDA(cudaMemset(g.dev, 0, g.bytes));
+    std::lock_guard<std::mutex> lock(srv->mu);
+    *grid_id = srv->next_grid++;
+    srv->grids[*grid_id] = g;
+    return IDG_OK;
+}
+
+IDG_API int idg_server_grid_read(idg_server *srv, int64_t grid_id, void *host_out) {
+    if (!srv || !host_out) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::unique_lock<std::mutex> lock(srv->mu);
+    auto it = srv->grids.find(grid_id);
+    if (it == srv->grids.end()) return fail(IDG_ERR_NOT_FOUND, "unknown grid %lld", (long long)grid_id);
+    std::vector<cudaEvent_t> wait = it->second.holders;
+    void *dev = it->second.dev;
+    const size_t bytes = it->second.bytes;
+    lock.unlock();
+    cudaSetDevice(srv->device);
+    for (cudaEvent_t e : wait) cudaEventSynchronize(e);
+    IDG_CUDA(cudaMemcpy(host_out, dev, bytes, cudaMemcpyDeviceToHost));
+    return IDG_OK;
+}
+
+IDG_API int idg_server_grid_release(idg_server *srv, int64_t grid_id) {
+    if (!srv) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL server");
+    std::lock_guard<std::mutex> lock(srv->mu);
+    auto it = srv->grids.find(grid_id);
+    if (it == srv->grids.end()) return fail(IDG_ERR_NOT_FOUND, "unknown grid %lld", (long long)grid_id);
+    if (!it->second.holders.empty()) return fail(IDG_ERR_REJECTED, "grid %lld has jobs in flight", (long long)grid_id);
+    for (auto &q : srv->queue)
+        if (q->spec.grid_id == grid_id) return fail(IDG_ERR_REJECTED, "grid %lld has queued jobs", (long long)grid_id);
+    cudaSetDevice(srv->device);
+    cudaFree(it->second.dev);
+    srv->grids.erase(it);
+    return IDG_OK;
+}
+
+IDG_API int idg_server_submit(idg_server *srv, const idg_job *job, int64_t *job_id) {
+    if (!srv || !job_id) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL argument");
+    auto j = std::make_shared<Job>();
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        if (int rc = validate_job(srv, job)) return rc;
+    }
+    j->spec = *job;
+    const int64_t N = job->nr_subgrids;
+    j->md.assign(job->metadata, job->metadata + N);
+    if (job->ext) j->ext.assign(job->ext, job->ext + N);
+    std::vector<int64_t> cost(N);
+    for (int64_t s = 0; s < N; ++s) {
+        const int nc = job->ext ? job->ext[s].channel_end - job->ext[s].channel_begin : job->params.nr_channels;
+        cost[s] = (int64_t)job->metadata[s].nr_timesteps * nc;
+        j->nvis += cost[s];
+    }
+    j->work.resize(N);
+    std::iota(j->work.begin(), j->work.end(), 0);
+    std::stable_sort(j->work.begin(), j->work.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    j->footprint = job_layout(j->spec).total;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    if (j->footprint > (size_t)srv->cfg.hbm_budget_bytes) {
+        ++srv->rejected;
+        return fail(IDG_ERR_REJECTED, "job needs %zu bytes of device memory, the budget is %lld", j->footprint,
+                    (long long)srv->cfg.hbm_budget_bytes);
+    }
+    j->id = srv->next_job++;
+    j->t_submit = Clock::now();
+    if (!srv->have_first) {
+        srv->first_submit = j->t_submit;
+        srv->have_first = true;
+    }
+    srv->jobs[j->id] = j;
+    srv->queue.push_back(j);
+    *job_id = j->id;
+    srv->cv_work.notify_all();
+    return IDG_OK;
+}
+
+IDG_API int idg_server_wait(idg_server *srv, int64_t job_id, int64_t timeout_ms, idg_job_stats *stats) {
+    if (!srv) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL server");
+    std::unique_lock<std::mutex> lock(srv->mu);
+    auto it = srv->jobs.find(job_id);
+    if (it == srv->jobs.end()) return fail(IDG_ERR_NOT_FOUND, "unknown job %lld", (long long)job_id);
+    std::shared_ptr<Job> j = it->second;
+    const bool ok = srv->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms),
+                                          [&] { return j->finished; });
+    if (!ok) return fail(IDG_ERR_TIMEOUT, "job %lld not finished after %lld ms", (long long)job_id, (long long)timeout_ms);
+    if (stats) {
+        stats->queue_ms = ms_between(j->t_submit, j->t_admit);
+        stats->run_ms = ms_between(j->t_admit, j->t_done);
+        stats->latency_ms = ms_between(j->t_submit, j->t_done);
+        stats->visibilities = j->nvis;
+        stats->status = j->status;
+    }
+    srv->jobs.erase(job_id);
+    if (j->status != IDG_OK) return fail(j->status, "job %lld failed", (long long)job_id);
+    return IDG_OK;
+}
+
+IDG_API int idg_server_stats(idg_server *srv, idg_server_summary *out) {
+    if (!srv || !out) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> lock(srv->mu);
+    memset(out, 0, sizeof *out);
+    out->completed = srv->completed;
+    out->rejected = srv->rejected;
+    out->failed = srv->failed;
+    out->queued = (int64_t)srv->queue.size();
+    int running = 0;
+    for (auto &s : srv->slots)
+        if (s) ++running;
+    out->running = running;
+    out->hbm_in_use = (int64_t)srv->in_use;
+    out->hbm_peak = (int64_t)srv->peak_use;
+    std::vector<double> l = srv->latencies;
+    if (!l.empty()) {
+        std::sort(l.begin(), l.end());
+        auto pct = [&](double q) { return l[std::min(l.size() - 1, (size_t)(q * (l.size() - 1) + 0.5))]; };
+        out->p50_ms = pct(0.50);
+        out->p99_ms = pct(0.99);
+        out->mean_ms = std::accumulate(l.begin(), l.end(), 0.0) / l.size();
+        const double span_s = ms_between(srv->first_submit, srv->last_done) * 1e-3;
+        out->mvis_per_s = span_s > 0 ? srv->total_vis / span_s / 1e6 : 0;
+    }
+    return IDG_OK;
+}
+
+} // extern "C"

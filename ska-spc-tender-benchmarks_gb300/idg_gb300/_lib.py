@@ -83,6 +83,60 @@ class IdgCycleTiming(ctypes.Structure):
     ]
 
 
+class IdgServerConfig(ctypes.Structure):
+    _fields_ = [("max_slots", ctypes.c_int32), ("cta_share", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64)]
+
+
+class IdgJob(ctypes.Structure):
+    _fields_ = [
+        ("op", ctypes.c_int32),
+        ("variant", ctypes.c_int32),
+        ("params", IdgParams),
+        ("nr_subgrids", ctypes.c_int64),
+        ("metadata", ctypes.c_void_p),
+        ("ext", ctypes.c_void_p),
+        ("nr_rows", ctypes.c_int64),
+        ("uvw", ctypes.c_void_p),
+        ("wavenumbers", ctypes.c_void_p),
+        ("vis_in", ctypes.c_void_p),
+        ("vis_out", ctypes.c_void_p),
+        ("spheroidal", ctypes.c_void_p),
+        ("aterms", ctypes.c_void_p),
+        ("grid_id", ctypes.c_int64),
+    ]
+
+
+class IdgJobStats(ctypes.Structure):
+    _fields_ = [
+        ("queue_ms", ctypes.c_double),
+        ("run_ms", ctypes.c_double),
+        ("latency_ms", ctypes.c_double),
+        ("visibilities", ctypes.c_int64),
+        ("status", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class IdgServerSummary(ctypes.Structure):
+    _fields_ = [
+        ("completed", ctypes.c_int64),
+        ("rejected", ctypes.c_int64),
+        ("failed", ctypes.c_int64),
+        ("queued", ctypes.c_int64),
+        ("running", ctypes.c_int64),
+        ("hbm_in_use", ctypes.c_int64),
+        ("hbm_peak", ctypes.c_int64),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
+        ("mvis_per_s", ctypes.c_double),
+    ]
+
+
+IDG_JOB_GRID = 0
+IDG_JOB_DEGRID = 1
+
+
 class IdgLaunchConfig(ctypes.Structure):
     _fields_ = [
         ("niterations", ctypes.c_int64),
@@ -125,6 +179,22 @@ _SIGNATURES = {
     "idg_imaging_cycle": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64,
                           ctypes.c_void_p],
     "idg_release_buffers": [],
+    "idg_plan_create": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, ctypes.POINTER(ctypes.c_void_p)],
+    "idg_plan_destroy": [_P],
+    "idg_plan_set_cta_limit": [_P, _I32],
+    "idg_plan_grid": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "idg_plan_degrid": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "idg_plan_capture_cycle": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "idg_plan_launch_cycle": [_P, _P],
+    "idg_plan_status": [_P, _P, ctypes.POINTER(ctypes.c_uint32), _I32],
+    "idg_server_create": [ctypes.POINTER(IdgServerConfig), ctypes.POINTER(ctypes.c_void_p)],
+    "idg_server_destroy": [_P],
+    "idg_server_grid_create": [_P, _I32, _I32, ctypes.POINTER(ctypes.c_int64)],
+    "idg_server_grid_read": [_P, _I64, _P],
+    "idg_server_grid_release": [_P, _I64],
+    "idg_server_submit": [_P, ctypes.POINTER(IdgJob), ctypes.POINTER(ctypes.c_int64)],
+    "idg_server_wait": [_P, _I64, _I64, ctypes.POINTER(IdgJobStats)],
+    "idg_server_stats": [_P, ctypes.POINTER(IdgServerSummary)],
     "idg_gridding_launch": [ctypes.POINTER(IdgLaunchConfig), _P, _P, _P, _P, _P, _P, _P, _P, _P,
                             ctypes.POINTER(IdgBenchmarkResult)],
     "idg_degridding_launch": [ctypes.POINTER(IdgLaunchConfig), _P, _P, _P, _P, _P, _P, _P, _P, _P,

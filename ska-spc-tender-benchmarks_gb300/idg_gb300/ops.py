@@ -76,6 +76,10 @@ def _check_common(spec: GridSpec, metadata, uvw, wavenumbers, vis, taper, aterms
     _req(metadata, "metadata", torch.int32)
     if metadata.dim() != 2 or metadata.shape[1] != 9:
         raise ValueError("metadata must be [N, 9] int32 (36-byte entries)")
+    _check_data(spec, uvw, wavenumbers, vis, taper, aterms)
+
+
+def _check_data(spec: GridSpec, uvw, wavenumbers, vis, taper, aterms):
     _req(uvw, "uvw", torch.float32)
     if uvw.dim() != 2 or uvw.shape[1] != 3:
         raise ValueError("uvw must be [rows, 3] float32")
@@ -192,6 +196,74 @@ def imaging_cycle(spec: GridSpec, metadata: np.ndarray, uvw: np.ndarray, wavenum
               int(chunk_subgrids), ctypes.byref(t))
     return {"total_ms": t.total_ms, "gridding_ms": t.gridding_ms, "degridding_ms": t.degridding_ms,
             "h2d_bytes": t.h2d_bytes, "d2h_bytes": t.d2h_bytes, "kernel_launches": t.kernel_launches}
+
+
+class Plan:
+    """A device-resident execution plan (idg_plan_*): metadata, longest-first work
+    list and subgrid work space on the device; optional CUDA graph of one cycle."""
+
+    def __init__(self, spec: GridSpec, metadata: np.ndarray, nr_rows: int, ext: np.ndarray | None = None,
+                 variant: int = VARIANT_BATCHED):
+        self.spec = spec
+        self._md = np.ascontiguousarray(metadata, dtype=_lib.METADATA_DTYPE)
+        self._ext = None if ext is None else np.ascontiguousarray(ext, dtype=_lib.SUBGRID_EXT_DTYPE)
+        self.nr_subgrids = int(self._md.shape[0])
+        self.nr_rows = int(nr_rows)
+        self._p = spec.to_c()
+        h = ctypes.c_void_p()
+        _lib.call("idg_plan_create", ctypes.byref(self._p), variant, self.nr_subgrids, ptr(self._md), ptr(self._ext),
+                  self.nr_rows, ctypes.byref(h))
+        self._h = h
+        self._keep = None
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().idg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_cta_limit(self, max_ctas: int) -> None:
+        _lib.call("idg_plan_set_cta_limit", self._h, int(max_ctas))
+
+    def _check(self, uvw, wavenumbers, vis, taper, aterms, grid):
+        _check_data(self.spec, uvw, wavenumbers, vis, taper, aterms)
+        S, G, W = self.spec.subgrid_size, self.spec.grid_size, self.spec.nr_w_planes
+        _req(grid, "grid", torch.complex64, (W, 4, G, G))
+        if uvw.shape[0] != self.nr_rows:
+            raise ValueError(f"uvw has {uvw.shape[0]} rows, the plan was built for {self.nr_rows}")
+
+    def grid(self, uvw, wavenumbers, vis, taper, aterms, grid, stream=None):
+        self._check(uvw, wavenumbers, vis, taper, aterms, grid)
+        _lib.call("idg_plan_grid", self._h, ptr(uvw), ptr(wavenumbers), ptr(vis), ptr(taper), ptr(aterms), ptr(grid),
+                  _stream_handle(stream))
+        return grid
+
+    def degrid(self, uvw, wavenumbers, vis_out, taper, aterms, grid, stream=None):
+        self._check(uvw, wavenumbers, vis_out, taper, aterms, grid)
+        _lib.call("idg_plan_degrid", self._h, ptr(uvw), ptr(wavenumbers), ptr(vis_out), ptr(taper), ptr(aterms),
+                  ptr(grid), _stream_handle(stream))
+        return vis_out
+
+    def capture_cycle(self, uvw, wavenumbers, vis_in, taper, aterms, grid, vis_out):
+        """Capture zero-grid + grid + degrid on these buffers as a CUDA graph."""
+        self._check(uvw, wavenumbers, vis_in, taper, aterms, grid)
+        _req(vis_out, "vis_out", torch.complex64, tuple(vis_in.shape))
+        _lib.call("idg_plan_capture_cycle", self._h, ptr(uvw), ptr(wavenumbers), ptr(vis_in), ptr(taper), ptr(aterms),
+                  ptr(grid), ptr(vis_out))
+        self._keep = (uvw, wavenumbers, vis_in, taper, aterms, grid, vis_out)  # the graph holds raw addresses
+
+    def launch_cycle(self, stream=None):
+        _lib.call("idg_plan_launch_cycle", self._h, _stream_handle(stream))
+
+    def status(self, clear: bool = True, stream=None) -> int:
+        v = ctypes.c_uint32(0)
+        _lib.call("idg_plan_status", self._h, _stream_handle(stream), ctypes.byref(v), 1 if clear else 0)
+        return int(v.value)
 
 
 def release_buffers() -> None:

@@ -309,3 +309,53 @@ def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
     assert tuning.get_shapes(S) == (res["gridder"], res["degridder"])
     assert res["gridder_ms"][res["gridder"]] == min(res["gridder_ms"])
     tuning.set_shapes(S, 0, 0)
+
+
+def test_plan_steps_and_graph_cycle_match_direct_calls(oracle_mod, idg):
+    """A plan's grid/degrid steps and its captured CUDA-graph cycle reproduce the
+    direct entry points; an uneven plan (longest-first work list) stays within tolerance."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    spec = D.config1()
+    spec.aterm_sigma = 0.05
+    obs = D.make_observation(spec)
+    vis = _vis(spec, seed=31)
+    S, G = spec.subgrid_size, spec.grid_size
+    gs = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    d = {k: dev(v) for k, v in dict(md=obs.metadata, uvw=obs.uvw, k=obs.wavenumbers, vis=vis, taper=obs.taper,
+                                    at=obs.aterms).items()}
+    N = spec.n_subgrids
+    # direct calls
+    sub = torch.empty((N, 4, S, S), dtype=torch.complex64, device="cuda")
+    g_ref = torch.zeros((1, 4, G, G), dtype=torch.complex64, device="cuda")
+    ops.grid_visibilities(gs, d["md"], d["uvw"], d["k"], d["vis"], d["taper"], d["at"], sub, g_ref)
+    v_ref = torch.zeros_like(d["vis"])
+    ops.degrid_visibilities(gs, d["md"], d["uvw"], d["k"], v_ref, d["taper"], d["at"], sub, g_ref)
+    torch.cuda.synchronize()
+    # oracle of the gridding step: gridder (no taper) -> DFT (+1, taper) -> adder
+    prm = oracle_mod.params(G, S, spec.nchannels, spec.nstations, N, spec.image_size)
+    ones = np.ones((S, S), np.float32)
+    want_grid = oracle_mod.adder(oracle_mod.subgrid_dft(
+        oracle_mod.gridder(prm, obs.uvw, obs.wavenumbers, vis, ones, obs.aterms, obs.metadata), +1, obs.taper),
+        obs.metadata, G)
+    check_rel("grid step vs oracle", g_ref.cpu().numpy(), want_grid, TOL)
+    for variant in VARIANTS:
+        plan = ops.Plan(gs, obs.metadata, spec.n_rows, variant=variant)
+        g = torch.zeros_like(g_ref)
+        plan.grid(d["uvw"], d["k"], d["vis"], d["taper"], d["at"], g)
+        v = torch.zeros_like(d["vis"])
+        plan.degrid(d["uvw"], d["k"], v, d["taper"], d["at"], g)
+        torch.cuda.synchronize()
+        check_rel(f"plan grid v{variant}", g.cpu().numpy(), g_ref.cpu().numpy(), TOL)
+        check_rel(f"plan degrid v{variant}", v.cpu().numpy(), v_ref.cpu().numpy(), TOL)
+        g2 = torch.full_like(g_ref, 7.0)
+        v2 = torch.zeros_like(d["vis"])
+        plan.capture_cycle(d["uvw"], d["k"], d["vis"], d["taper"], d["at"], g2, v2)
+        for _ in range(2):
+            plan.launch_cycle()
+        torch.cuda.synchronize()
+        check_rel(f"graph cycle grid v{variant}", g2.cpu().numpy(), g_ref.cpu().numpy(), TOL)
+        check_rel(f"graph cycle vis v{variant}", v2.cpu().numpy(), v_ref.cpu().numpy(), TOL)
+        assert plan.status() == 0
+        plan.close()

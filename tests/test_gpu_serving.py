@@ -1,0 +1,113 @@
+"""Serving: jobs admitted while others run give the same results as the same
+jobs run alone (within the parity tolerance -- the adder accumulates with
+floating-point atomics, so the grid's summation order may differ), jobs
+larger than the HBM budget are rejected, and latency statistics are kept."""
+import numpy as np
+import pytest
+import torch
+
+import idg_gb300._lib as L
+from conftest import check_rel
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def _job(seed, nstations, ntimesteps, nchannels, grid_size=1024):
+    from idg_gb300 import datasets as D
+    from idg_gb300.ops import GridSpec
+    from idg_gb300.serving import JobData
+
+    spec = D.ObservationSpec(nstations=nstations, disk_radius_m=2000.0, ntimesteps=ntimesteps,
+                             timesteps_per_subgrid=32, nchannels=nchannels, f_start=150e6, f_end=160e6,
+                             subgrid_size=32, grid_size=grid_size, image_size=0.05, aterm_sigma=0.05,
+                             aterm_interval=64, seed=seed)
+    obs = D.make_observation(spec)
+    rng = np.random.default_rng(seed)
+    vis = (rng.standard_normal((spec.n_rows, nchannels, 4)) + 1j * rng.standard_normal((spec.n_rows, nchannels, 4))).astype(np.complex64)
+    gs = GridSpec(grid_size, 32, nchannels, nstations, obs.aterms.shape[0], 1, spec.image_size)
+    grid_in = JobData(gs, obs.metadata, obs.uvw, obs.wavenumbers, obs.taper, np.ascontiguousarray(obs.aterms), vis)
+    out = np.zeros_like(vis)
+    degrid = JobData(gs, obs.metadata, obs.uvw, obs.wavenumbers, obs.taper, np.ascontiguousarray(obs.aterms), out)
+    return grid_in, degrid
+
+
+JOBS = [(1, 6, 128, 16), (2, 9, 96, 8), (3, 5, 256, 24), (4, 8, 64, 16)]
+
+
+def _run(server, jobs, together):
+    """Grid every job into its own resident grid, then degrid from it."""
+    from idg_gb300.serving import Server  # noqa: F401
+
+    grids = [server.grid_create(1024) for _ in jobs]
+    if together:
+        ids = [server.submit(L.IDG_JOB_GRID, g, gid) for (g, _), gid in zip(jobs, grids)]
+        ids += [server.submit(L.IDG_JOB_DEGRID, d, gid) for (_, d), gid in zip(jobs, grids)]
+        for i in ids:
+            server.wait(i, 120)
+    else:
+        for (g, d), gid in zip(jobs, grids):
+            server.wait(server.submit(L.IDG_JOB_GRID, g, gid), 120)
+            server.wait(server.submit(L.IDG_JOB_DEGRID, d, gid), 120)
+    out = [(server.grid_read(gid, 1024), d.vis.copy()) for (_, d), gid in zip(jobs, grids)]
+    for gid in grids:
+        server.grid_release(gid)
+    return out
+
+
+def test_jobs_alone_and_in_the_mix_agree(idg):
+    from idg_gb300.serving import Server
+
+    jobs = [_job(*j) for j in JOBS]
+    with Server(max_slots=1, hbm_budget_bytes=8 << 30) as s1:
+        alone = _run(s1, jobs, together=False)
+        st1 = s1.stats()
+    for _, d in jobs:
+        d.vis[...] = 0
+    with Server(max_slots=4, hbm_budget_bytes=8 << 30, cta_share=True) as s4:
+        mixed = _run(s4, jobs, together=True)
+        st4 = s4.stats()
+    for k, ((ga, va), (gm, vm)) in enumerate(zip(alone, mixed)):
+        assert np.abs(ga).max() > 0 and np.abs(va).max() > 0
+        check_rel(f"serving job {k} grid alone vs mix", gm, ga, TOL)
+        check_rel(f"serving job {k} vis alone vs mix", vm, va, TOL)
+    assert st1["completed"] == st4["completed"] == 2 * len(JOBS)
+    assert st4["p99_ms"] >= st4["p50_ms"] > 0
+    assert st4["hbm_peak"] > 0
+
+
+def test_serving_result_matches_direct_plan(idg):
+    """A served gridding + degridding job equals the plan API on the same data."""
+    from idg_gb300 import ops
+    from idg_gb300.serving import Server
+
+    g, d = _job(7, 6, 128, 16)
+    with Server(max_slots=2, hbm_budget_bytes=4 << 30) as s:
+        gid = s.grid_create(1024)
+        s.wait(s.submit(L.IDG_JOB_GRID, g, gid), 120)
+        s.wait(s.submit(L.IDG_JOB_DEGRID, d, gid), 120)
+        grid_srv = s.grid_read(gid, 1024)
+    dv = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in
+          dict(uvw=g.uvw, k=g.wavenumbers, vis=g.vis, taper=g.taper, at=g.aterms).items()}
+    plan = ops.Plan(g.spec, g.metadata, g.nr_rows)
+    grid = torch.zeros((1, 4, 1024, 1024), dtype=torch.complex64, device="cuda")
+    plan.grid(dv["uvw"], dv["k"], dv["vis"], dv["taper"], dv["at"], grid)
+    vout = torch.zeros_like(dv["vis"])
+    plan.degrid(dv["uvw"], dv["k"], vout, dv["taper"], dv["at"], grid)
+    torch.cuda.synchronize()
+    check_rel("served grid vs plan", grid_srv, grid.cpu().numpy(), TOL)
+    check_rel("served vis vs plan", d.vis, vout.cpu().numpy(), TOL)
+    plan.close()
+
+
+def test_job_over_budget_is_rejected(idg):
+    from idg_gb300.serving import Server
+
+    g, _ = _job(5, 8, 256, 16)
+    with Server(max_slots=2, hbm_budget_bytes=16 << 20) as s:
+        gid = s.grid_create(1024)
+        with pytest.raises(L.IdgError) as e:
+            s.submit(L.IDG_JOB_GRID, g, gid)
+        assert e.value.code == L.IDG_ERR_REJECTED
+        assert s.stats()["rejected"] == 1
