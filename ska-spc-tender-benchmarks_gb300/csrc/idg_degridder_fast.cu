@@ -62,18 +62,26 @@ __device__ __forceinline__ f2 reduce_2pi(f2 x) {
     return ffma2(k, pack2(-k2PiLo, -k2PiLo), x);
 }
 
+template <bool FTZ>
 __device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
     float x0, x1, s0, c0, s1, c1;
     unpack2(x, x0, x1);
-    __sincosf(x0, &s0, &c0);
-    __sincosf(x1, &s1, &c1);
+    if (FTZ) {
+        s0 = sin_ftz(x0);
+        c0 = cos_ftz(x0);
+        s1 = sin_ftz(x1);
+        c1 = cos_ftz(x1);
+    } else {
+        __sincosf(x0, &s0, &c0);
+        __sincosf(x1, &s1, &c1);
+    }
     c = pack2(c0, c1);
     s = pack2(s0, s1);
 }
 
 // Kernel shape: NT threads per CTA, BATCH pixel pairs staged per pass, at least
-// MINB CTAs per SM (register cap).
-template <int NT, int BATCH, int MINB>
+// MINB CTAs per SM (register cap); FTZ: SFU sine/cosine flushing subnormals.
+template <int NT, int BATCH, int MINB, bool FTZ>
 __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) {
     constexpr int kT = NT, kBatchPairs = BATCH;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -229,7 +237,7 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
                             f2 x = ffma2(kc[j], Q, tau0);
                             if (!fast) x = reduce_2pi(x);
                             f2 C, Sn;
-                            sincos_pair(x, C, Sn);
+                            sincos_pair<FTZ>(x, C, Sn);
                             // V += P (cos - i sin): re += pr c + pi s ; im += pi c - pr s
                             acc[j][0] = ffma2(pi0, Sn, ffma2(pr0, C, acc[j][0]));
                             acc[j][1] = ffma2(nr0, Sn, ffma2(pi0, C, acc[j][1]));
@@ -277,9 +285,9 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
     }
 }
 
-template <int NT, int BATCH, int MINB>
+template <int NT, int BATCH, int MINB, bool FTZ = false>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
-    auto kern = degridder_fast_kernel<NT, BATCH, MINB>;
+    auto kern = degridder_fast_kernel<NT, BATCH, MINB, FTZ>;
     const size_t smem = layout(a.S, a.C, BATCH).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -299,7 +307,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 } // namespace
 
 // Launch shapes of the batched degridder (index = shape id).
-int degridder_fast_shapes() { return 5; }
+int degridder_fast_shapes() { return 7; }
 
 cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -307,6 +315,8 @@ cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int 
     case 2: return launch_shape<256, 512, 2>(a, stream); // 16 warps/SM in 256-thread CTAs
     case 3: return launch_shape<128, 256, 4>(a, stream); // smaller staging batches
     case 4: return launch_shape<128, 512, 2>(a, stream); // 8 warps/SM, registers uncapped
+    case 5: return launch_shape<128, 512, 2, true>(a, stream); // shape 4, subnormal-flushing SFU sin/cos
+    case 6: return launch_shape<128, 512, 3, true>(a, stream); // shape 0, subnormal-flushing SFU sin/cos
     default: return launch_shape<128, 512, 3>(a, stream); // 12 warps/SM
     }
 }

@@ -73,24 +73,34 @@ __device__ __forceinline__ f2 reduce_2pi(f2 x) {
     return ffma2(k, pack2(-k2PiLo, -k2PiLo), x);
 }
 
+// FTZ: the SFU instructions flushing subnormal arguments (sin/cos.approx.ftz)
+// instead of __sincosf's default that honours them.
+template <bool FTZ = false>
 __device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
     float x0, x1, s0, c0, s1, c1;
     unpack2(x, x0, x1);
-    __sincosf(x0, &s0, &c0);
-    __sincosf(x1, &s1, &c1);
+    if (FTZ) {
+        s0 = sin_ftz(x0);
+        c0 = cos_ftz(x0);
+        s1 = sin_ftz(x1);
+        c1 = cos_ftz(x1);
+    } else {
+        __sincosf(x0, &s0, &c0);
+        __sincosf(x1, &s1, &c1);
+    }
     c = pack2(c0, c1);
     s = pack2(s0, s1);
 }
 
 // Phasors of one channel for all pixel pairs of the thread.
-template <int PAIRS, bool FAST>
+template <int PAIRS, bool FAST, bool FTZ>
 __device__ __forceinline__ void channel_phasors(f2 kc, const f2 (&tau0)[PAIRS], const f2 (&Q)[PAIRS], f2 (&C)[PAIRS],
                                                 f2 (&Sn)[PAIRS]) {
 #pragma unroll
     for (int j = 0; j < PAIRS; ++j) {
         f2 x = ffma2(kc, Q[j], tau0[j]);
         if (!FAST) x = reduce_2pi(x);
-        sincos_pair(x, C[j], Sn[j]);
+        sincos_pair<FTZ>(x, C[j], Sn[j]);
     }
 }
 
@@ -121,7 +131,8 @@ __device__ __forceinline__ void channel_macs(f2 (&acc)[PAIRS][8], const float4 *
 // One staged tile: tt timesteps x ncc channels.
 // PIPE = 1: the channel loop is software pipelined -- the sincos of channel c+1
 // is issued before the MACs of channel c, so a warp keeps SFU and FMA work in
-// flight together (more registers).  PIPE = 0: phasors then MACs per channel.
+// flight together (more registers).  PIPE & 1 = 0: phasors then MACs per
+// channel.  PIPE & 2: SFU sine/cosine with subnormal flushing.
 template <int PAIRS, bool FAST, int PIPE>
 __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[PAIRS], const float4 *coef,
                                           const f2 *geo, const float4 *vexp, const f2 *kp, int tt, int ncc) {
@@ -137,9 +148,10 @@ __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[P
             Q[j] = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
         }
         const float4 *vt = vexp + (size_t)t * ncc * 6;
-        if (PIPE) {
+        constexpr bool FTZ = (PIPE & 2) != 0;
+        if (PIPE & 1) {
             f2 Cn[PAIRS], Sn[PAIRS];
-            channel_phasors<PAIRS, FAST>(kp[0], tau0, Q, Cn, Sn);
+            channel_phasors<PAIRS, FAST, FTZ>(kp[0], tau0, Q, Cn, Sn);
 #pragma unroll 1
             for (int c = 0; c + 1 < ncc; ++c) {
                 f2 C[PAIRS], S[PAIRS];
@@ -148,7 +160,7 @@ __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[P
                     C[j] = Cn[j];
                     S[j] = Sn[j];
                 }
-                channel_phasors<PAIRS, FAST>(kp[c + 1], tau0, Q, Cn, Sn);
+                channel_phasors<PAIRS, FAST, FTZ>(kp[c + 1], tau0, Q, Cn, Sn);
                 channel_macs<PAIRS>(acc, vt + 6 * c, C, S);
             }
             channel_macs<PAIRS>(acc, vt + 6 * (ncc - 1), Cn, Sn);
@@ -156,7 +168,7 @@ __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[P
 #pragma unroll 1
             for (int c = 0; c < ncc; ++c) {
                 f2 C[PAIRS], S[PAIRS];
-                channel_phasors<PAIRS, FAST>(kp[c], tau0, Q, C, S);
+                channel_phasors<PAIRS, FAST, FTZ>(kp[c], tau0, Q, C, S);
                 channel_macs<PAIRS>(acc, vt + 6 * c, C, S);
             }
         }
@@ -367,6 +379,8 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 //   2: 128 x 2, 128-visibility tiles, 4 CTAs/SM (16 warps), pipelined
 //   3: 256 x 2, 256-visibility tiles, 2 CTAs/SM (16 warps), pipelined
 //   4: 128 x 2, 128-visibility tiles, 4 CTAs/SM (16 warps), plain channel loop
+//   5: shape 0 with the subnormal-flushing SFU sine/cosine
+//   6: shape 1 with the subnormal-flushing SFU sine/cosine
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -388,7 +402,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return 5; }
+int gridder_fast_shapes() { return 7; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -396,6 +410,8 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 2: return launch_shape<128, 2, 128, 4, 1>(a, stream);
     case 3: return launch_shape<256, 2, 256, 2, 1>(a, stream);
     case 4: return launch_shape<128, 2, 128, 4, 0>(a, stream);
+    case 5: return launch_shape<128, 4, 256, 3, 2>(a, stream);
+    case 6: return launch_shape<128, 4, 256, 2, 3>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }

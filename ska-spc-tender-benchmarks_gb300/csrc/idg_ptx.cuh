@@ -42,6 +42,19 @@ __device__ __forceinline__ f2 fsub2(f2 a, f2 b) {
     return d;
 }
 
+// SFU sine and cosine (radians), flushing subnormal inputs to zero; the phases
+// here are never subnormal in any meaningful way (sin x = x there anyway).
+__device__ __forceinline__ float sin_ftz(float x) {
+    float r;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float cos_ftz(float x) {
+    float r;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // mbarrier + bulk async copy (global -> shared, completion counted in bytes)
 // ---------------------------------------------------------------------------

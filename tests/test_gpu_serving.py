@@ -104,8 +104,8 @@ def test_serving_result_matches_direct_plan(idg):
 def test_job_over_budget_is_rejected(idg):
     from idg_gb300.serving import Server
 
-    g, _ = _job(5, 8, 256, 16)
-    with Server(max_slots=2, hbm_budget_bytes=16 << 20) as s:
+    g, _ = _job(5, 8, 256, 16)  # ~11 MB of device memory
+    with Server(max_slots=2, hbm_budget_bytes=4 << 20) as s:
         gid = s.grid_create(1024)
         with pytest.raises(L.IdgError) as e:
             s.submit(L.IDG_JOB_GRID, g, gid)
