@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of each baseline half")
     ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline (profiling runs)")
     ap.add_argument("--max-subgrids", type=int, default=0, help="use only the first N subgrids of the plan (profiling)")
+    ap.add_argument("--shapes", default="", help="G,D: batched gridder/degridder launch shapes instead of autotuning")
     return ap.parse_args()
 
 
@@ -224,7 +225,13 @@ def run_ours(args, rank, world, local_rank):
 
     # autotune the batched kernels' launch shapes on a leading sample of the plan
     tune = None
-    if variant == ops.VARIANT_BATCHED:
+    if variant == ops.VARIANT_BATCHED and args.shapes:
+        from idg_gb300 import tuning
+
+        gsh, dsh = (int(x) for x in args.shapes.split(","))
+        tuning.set_shapes(S, gsh, dsh)
+        tune = {"gridder": gsh, "degridder": dsh, "fixed": True}
+    elif variant == ops.VARIANT_BATCHED:
         from idg_gb300 import tuning
 
         ns = min(N, 8192)

@@ -8,12 +8,14 @@
 //    taper applied) in shared memory as pixel PAIRS laid out for packed
 //    arithmetic: per pair and correlation (re_a, re_b, im_a, im_b) and
 //    (-re_a, -re_b); the pair's geometry (hx, hy, n) is staged once per CTA.
-//  * A visibility group is one timestep x 4 channels.  Four lanes share a
-//    group, each summing a quarter of the pixel pairs; a lane keeps the
-//    group's 4 x 4 complex partial sums as packed pairs (one half per pixel of
-//    the pair) and so issues two fma.rn.f32x2 per complex MAC of two pixels.
+//  * A visibility group is one timestep x CB channels (CB = 4 or 8).  Four
+//    lanes share a group, each summing a quarter of the pixel pairs; a lane
+//    keeps the group's CB x 4 complex partial sums as packed pairs (one half
+//    per pixel of the pair) and so issues two fma.rn.f32x2 per complex MAC of
+//    two pixels (or, in the Gauss variant, three per two complex MACs).
 //  * At the end of a group the two halves are added and the four lanes'
-//    partial sums are combined with warp shuffles; each lane writes 1 channel.
+//    partial sums are combined with warp shuffles; each lane writes CB/4
+//    channels.
 //  * Phase handling is the gridder's (idg_gridder_fast.cu): FP64 per-tile
 //    coefficients, tau0 reduced to [-pi, pi] per (pair, timestep), and the
 //    per-channel sincos unreduced when the tile's bound allows.
@@ -25,7 +27,7 @@ namespace idg {
 
 namespace {
 
-constexpr int kCB = 4;                  // channels per group (one per lane of the group at write-out)
+constexpr int kMaxCB = 8;               // channels per visibility group, at most (template CB = 4 or 8)
 constexpr int kLanesPerGroup = 4;
 constexpr int kGroupsPerWarp = 32 / kLanesPerGroup;
 constexpr int kTimeTile = 64;
@@ -49,7 +51,7 @@ __host__ __device__ inline Layout layout(int S, int C, int batch_pairs) {
     L.pix = off;   off += (size_t)batch_pairs * 96;          // 4 x (re_a,re_b,im_a,im_b) + 2 x (-re pairs)
     L.geo = off;   off += (size_t)(S * S / 2) * 24;          // (hx_a,hx_b) (hy,hy) (n_a,n_b)
     L.coef = off;  off += (size_t)kTimeTile * 48;            // (a,a,b,b) (g,g,qu,qu) (qv,qv,qw,qw)
-    L.kappa = off; off += (size_t)(C + kCB) * 4;             // kappa per channel, padded with zeros
+    L.kappa = off; off += (size_t)(C + kMaxCB) * 4;          // kappa per channel, padded with zeros
     L.total = (off + 15) & ~size_t(15);
     return L;
 }
@@ -79,11 +81,76 @@ __device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
     s = pack2(s0, s1);
 }
 
+// Kernel variant bits (the FLAGS template argument).
+constexpr int kFtz = 2;    // SFU sine/cosine flushing subnormal arguments
+constexpr int kGauss = 4;  // three-multiplication MACs (12 accumulators per channel)
+constexpr int kUnroll2 = 8; // pixel-pair loop unrolled by two
+
+// Partial visibilities of one pixel pair for the group's channels (four complex
+// MACs per correlation):  V += P (cos - i sin).
+template <int kCB, bool FAST, bool FTZ>
+__device__ __forceinline__ void pair_macs(f2 (&acc)[kCB][8], const f2 (&kc)[kCB], f2 tau0, f2 Q, const float4 *d) {
+    const float4 e0 = d[0], e1 = d[1], e2 = d[2], e3 = d[3], e4 = d[4], e5 = d[5];
+    const f2 pr0 = pack2(e0.x, e0.y), pi0 = pack2(e0.z, e0.w);
+    const f2 pr1 = pack2(e1.x, e1.y), pi1 = pack2(e1.z, e1.w);
+    const f2 pr2 = pack2(e2.x, e2.y), pi2 = pack2(e2.z, e2.w);
+    const f2 pr3 = pack2(e3.x, e3.y), pi3 = pack2(e3.z, e3.w);
+    const f2 nr0 = pack2(e4.x, e4.y), nr1 = pack2(e4.z, e4.w);
+    const f2 nr2 = pack2(e5.x, e5.y), nr3 = pack2(e5.z, e5.w);
+#pragma unroll
+    for (int j = 0; j < kCB; ++j) {
+        f2 x = ffma2(kc[j], Q, tau0);
+        if (!FAST) x = reduce_2pi(x);
+        f2 C, Sn;
+        sincos_pair<FTZ>(x, C, Sn);
+        // re += pr c + pi s ; im += pi c - pr s
+        acc[j][0] = ffma2(pi0, Sn, ffma2(pr0, C, acc[j][0]));
+        acc[j][1] = ffma2(nr0, Sn, ffma2(pi0, C, acc[j][1]));
+        acc[j][2] = ffma2(pi1, Sn, ffma2(pr1, C, acc[j][2]));
+        acc[j][3] = ffma2(nr1, Sn, ffma2(pi1, C, acc[j][3]));
+        acc[j][4] = ffma2(pi2, Sn, ffma2(pr2, C, acc[j][4]));
+        acc[j][5] = ffma2(nr2, Sn, ffma2(pi2, C, acc[j][5]));
+        acc[j][6] = ffma2(pi3, Sn, ffma2(pr3, C, acc[j][6]));
+        acc[j][7] = ffma2(nr3, Sn, ffma2(pi3, C, acc[j][7]));
+    }
+}
+
+// Gauss form of pair_macs: with the pixel a + ib and the phasor c + id =
+// cos - i sin, k1 = a (c + d) = a (cos - sin), -k2 = (a + b) sin,
+// k3 = (b - a) cos; Re = k1 + (-k2), Im = k1 + k3.  The staged operands per
+// correlation are the pixel-pair vectors a, a + b, b - a.
+template <int kCB, bool FAST, bool FTZ>
+__device__ __forceinline__ void pair_macs(f2 (&acc)[kCB][12], const f2 (&kc)[kCB], f2 tau0, f2 Q, const float4 *d) {
+    const uint32_t base = smem_addr(d);
+    f2 o[12];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) lds2(base + 16 * q, o[2 * q], o[2 * q + 1]);
+#pragma unroll
+    for (int j = 0; j < kCB; ++j) {
+        f2 x = ffma2(kc[j], Q, tau0);
+        if (!FAST) x = reduce_2pi(x);
+        f2 C, Sn;
+        sincos_pair<FTZ>(x, C, Sn);
+        const f2 cms = fsub2(C, Sn);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            acc[j][3 * k] = ffma2(o[3 * k], cms, acc[j][3 * k]);
+            acc[j][3 * k + 1] = ffma2(o[3 * k + 1], Sn, acc[j][3 * k + 1]);
+            acc[j][3 * k + 2] = ffma2(o[3 * k + 2], C, acc[j][3 * k + 2]);
+        }
+    }
+}
+
 // Kernel shape: NT threads per CTA, BATCH pixel pairs staged per pass, at least
-// MINB CTAs per SM (register cap); FTZ: SFU sine/cosine flushing subnormals.
-template <int NT, int BATCH, int MINB, bool FTZ>
+// MINB CTAs per SM (register cap), CB channels per visibility group (the
+// per-(pixel pair, timestep) phase terms are computed once per group, so a
+// larger group amortises them further); FLAGS: kFtz, kGauss.
+template <int NT, int BATCH, int MINB, int FLAGS, int CB>
 __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) {
-    constexpr int kT = NT, kBatchPairs = BATCH;
+    constexpr int kT = NT, kBatchPairs = BATCH, kCB = CB;
+    static_assert(CB == 4 || CB == 8, "channel groups of 4 or 8");
+    constexpr bool FTZ = (FLAGS & kFtz) != 0, kG = (FLAGS & kGauss) != 0;
+    constexpr int kAcc = kG ? 12 : 8;
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = a.S, S2 = S * S, npairs = S2 / 2;
     const Layout L = layout(S, a.C, BATCH);
@@ -165,11 +232,27 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
                         aterm_adjoint(v[h], j1, j2);
                 }
                 float4 *d = pix + 6 * i;
+                if (kG) {
+                    // per correlation the pair vectors a, a + b, b - a
+                    float e[12][2];
 #pragma unroll
-                for (int pol = 0; pol < 4; ++pol)
-                    d[pol] = make_float4(v[0][pol].re, v[1][pol].re, v[0][pol].im, v[1][pol].im);
-                d[4] = make_float4(-v[0][0].re, -v[1][0].re, -v[0][1].re, -v[1][1].re);
-                d[5] = make_float4(-v[0][2].re, -v[1][2].re, -v[0][3].re, -v[1][3].re);
+                    for (int pol = 0; pol < 4; ++pol)
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            e[3 * pol][h] = v[h][pol].re;
+                            e[3 * pol + 1][h] = v[h][pol].re + v[h][pol].im;
+                            e[3 * pol + 2][h] = v[h][pol].im - v[h][pol].re;
+                        }
+#pragma unroll
+                    for (int q = 0; q < 6; ++q)
+                        d[q] = make_float4(e[2 * q][0], e[2 * q][1], e[2 * q + 1][0], e[2 * q + 1][1]);
+                } else {
+#pragma unroll
+                    for (int pol = 0; pol < 4; ++pol)
+                        d[pol] = make_float4(v[0][pol].re, v[1][pol].re, v[0][pol].im, v[1][pol].im);
+                    d[4] = make_float4(-v[0][0].re, -v[1][0].re, -v[0][1].re, -v[1][1].re);
+                    d[5] = make_float4(-v[0][2].re, -v[1][2].re, -v[0][3].re, -v[1][3].re);
+                }
             }
 
             for (int t0 = 0; t0 < si.T; t0 += kTimeTile) {
@@ -213,41 +296,22 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
                         const float kv = kap[cfirst + j];
                         kc[j] = pack2(kv, kv);
                     }
-                    f2 acc[kCB][8];
+                    f2 acc[kCB][kAcc];
 #pragma unroll
                     for (int j = 0; j < kCB; ++j)
 #pragma unroll
-                        for (int r = 0; r < 8; ++r) acc[j][r] = 0ull;
+                        for (int r = 0; r < kAcc; ++r) acc[j][r] = 0ull;
 
+#pragma unroll((FLAGS & kUnroll2) ? 2 : 1)
                     for (int i = part; i < np; i += kLanesPerGroup) {
                         const int p = pb + i;
                         const f2 hx = geo[3 * p], hy = geo[3 * p + 1], nn = geo[3 * p + 2];
                         const f2 tau0 = reduce_2pi(ffma2(A2, hx, ffma2(B2, hy, fmul2(G2, nn))));
                         const f2 Q = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
-                        const float4 *d = pix + 6 * i;
-                        const float4 e0 = d[0], e1 = d[1], e2 = d[2], e3 = d[3], e4 = d[4], e5 = d[5];
-                        const f2 pr0 = pack2(e0.x, e0.y), pi0 = pack2(e0.z, e0.w);
-                        const f2 pr1 = pack2(e1.x, e1.y), pi1 = pack2(e1.z, e1.w);
-                        const f2 pr2 = pack2(e2.x, e2.y), pi2 = pack2(e2.z, e2.w);
-                        const f2 pr3 = pack2(e3.x, e3.y), pi3 = pack2(e3.z, e3.w);
-                        const f2 nr0 = pack2(e4.x, e4.y), nr1 = pack2(e4.z, e4.w);
-                        const f2 nr2 = pack2(e5.x, e5.y), nr3 = pack2(e5.z, e5.w);
-#pragma unroll
-                        for (int j = 0; j < kCB; ++j) {
-                            f2 x = ffma2(kc[j], Q, tau0);
-                            if (!fast) x = reduce_2pi(x);
-                            f2 C, Sn;
-                            sincos_pair<FTZ>(x, C, Sn);
-                            // V += P (cos - i sin): re += pr c + pi s ; im += pi c - pr s
-                            acc[j][0] = ffma2(pi0, Sn, ffma2(pr0, C, acc[j][0]));
-                            acc[j][1] = ffma2(nr0, Sn, ffma2(pi0, C, acc[j][1]));
-                            acc[j][2] = ffma2(pi1, Sn, ffma2(pr1, C, acc[j][2]));
-                            acc[j][3] = ffma2(nr1, Sn, ffma2(pi1, C, acc[j][3]));
-                            acc[j][4] = ffma2(pi2, Sn, ffma2(pr2, C, acc[j][4]));
-                            acc[j][5] = ffma2(nr2, Sn, ffma2(pi2, C, acc[j][5]));
-                            acc[j][6] = ffma2(pi3, Sn, ffma2(pr3, C, acc[j][6]));
-                            acc[j][7] = ffma2(nr3, Sn, ffma2(pi3, C, acc[j][7]));
-                        }
+                        if (fast)
+                            pair_macs<kCB, true, FTZ>(acc, kc, tau0, Q, pix + 6 * i);
+                        else
+                            pair_macs<kCB, false, FTZ>(acc, kc, tau0, Q, pix + 6 * i);
                     }
                     // fold the pair halves, then combine the four lanes of the group
                     float vsum[kCB][8];
@@ -256,7 +320,10 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
 #pragma unroll
                         for (int r = 0; r < 8; ++r) {
                             float lo, hi;
-                            unpack2(acc[j][r], lo, hi);
+                            if (kG) // Re = k1 + (-k2), Im = k1 + k3
+                                unpack2(fadd2(acc[j][3 * (r / 2)], acc[j][3 * (r / 2) + 1 + (r & 1)]), lo, hi);
+                            else
+                                unpack2(acc[j][r], lo, hi);
                             float v = lo + hi;
                             v += __shfl_xor_sync(0xffffffffu, v, 1);
                             v += __shfl_xor_sync(0xffffffffu, v, 2);
@@ -266,7 +333,7 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
                         float4 *row = a.vis + ((int64_t)si.row0 + t0 + t) * a.C * 2;
 #pragma unroll
                         for (int j = 0; j < kCB; ++j) {
-                            if (j != part || cfirst + j >= nc) continue;
+                            if (j % kLanesPerGroup != part || cfirst + j >= nc) continue;
                             const int c = si.c0 + cfirst + j;
                             float4 va = make_float4(vsum[j][0], vsum[j][1], vsum[j][2], vsum[j][3]);
                             float4 vb = make_float4(vsum[j][4], vsum[j][5], vsum[j][6], vsum[j][7]);
@@ -285,9 +352,9 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
     }
 }
 
-template <int NT, int BATCH, int MINB, bool FTZ = false>
+template <int NT, int BATCH, int MINB, int FLAGS = 0, int CB = 4>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
-    auto kern = degridder_fast_kernel<NT, BATCH, MINB, FTZ>;
+    auto kern = degridder_fast_kernel<NT, BATCH, MINB, FLAGS, CB>;
     const size_t smem = layout(a.S, a.C, BATCH).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -307,7 +374,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 } // namespace
 
 // Launch shapes of the batched degridder (index = shape id).
-int degridder_fast_shapes() { return 7; }
+int degridder_fast_shapes() { return 15; }
 
 cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -315,8 +382,16 @@ cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int 
     case 2: return launch_shape<256, 512, 2>(a, stream); // 16 warps/SM in 256-thread CTAs
     case 3: return launch_shape<128, 256, 4>(a, stream); // smaller staging batches
     case 4: return launch_shape<128, 512, 2>(a, stream); // 8 warps/SM, registers uncapped
-    case 5: return launch_shape<128, 512, 2, true>(a, stream); // shape 4, subnormal-flushing SFU sin/cos
-    case 6: return launch_shape<128, 512, 3, true>(a, stream); // shape 0, subnormal-flushing SFU sin/cos
+    case 5: return launch_shape<128, 512, 2, kFtz>(a, stream); // shape 4, subnormal-flushing SFU sin/cos
+    case 6: return launch_shape<128, 512, 3, kFtz>(a, stream); // shape 0, subnormal-flushing SFU sin/cos
+    case 7: return launch_shape<128, 512, 2, kGauss>(a, stream); // shape 4 with Gauss MACs
+    case 8: return launch_shape<128, 512, 3, kGauss>(a, stream); // shape 0 with Gauss MACs
+    case 9: return launch_shape<256, 512, 1, kGauss>(a, stream); // 8 warps/SM in 256-thread CTAs, Gauss MACs
+    case 10: return launch_shape<128, 512, 2, 0, 8>(a, stream); // shape 4 with 8-channel groups
+    case 11: return launch_shape<128, 512, 2, kGauss, 8>(a, stream); // shape 7 with 8-channel groups
+    case 12: return launch_shape<256, 512, 1, kGauss, 8>(a, stream); // shape 9 with 8-channel groups
+    case 13: return launch_shape<128, 512, 2, kUnroll2>(a, stream); // shape 4, pixel loop unrolled by two
+    case 14: return launch_shape<128, 512, 2, kUnroll2, 8>(a, stream); // shape 10, pixel loop unrolled by two
     default: return launch_shape<128, 512, 3>(a, stream); // 12 warps/SM
     }
 }

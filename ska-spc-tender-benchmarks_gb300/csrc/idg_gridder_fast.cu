@@ -104,6 +104,32 @@ __device__ __forceinline__ void channel_phasors(f2 kc, const f2 (&tau0)[PAIRS], 
     }
 }
 
+// Three-multiplication complex MAC (Gauss): with V = a + ib and the phasor
+// c + id,  k1 = a (c + d),  k2 = (a + b) d,  k3 = (b - a) c  give
+// Re(V e) = k1 - k2 and Im(V e) = k1 + k3.  The three products are summed
+// separately over all visibilities and combined once in the epilogue, so a
+// pixel pair costs 12 fma.rn.f32x2 + 1 add.rn.f32x2 per visibility instead
+// of 16.  Operands per visibility, pre-expanded per tile (duplicated into both
+// halves): for each correlation (a, a), (a + b, a + b), (b - a, b - a).
+template <int PAIRS>
+__device__ __forceinline__ void channel_macs(f2 (&acc)[PAIRS][12], const float4 *vv, const f2 (&C)[PAIRS],
+                                             const f2 (&Sn)[PAIRS]) {
+    const uint32_t base = smem_addr(vv);
+    f2 o[12];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) lds2(base + 16 * q, o[2 * q], o[2 * q + 1]);
+#pragma unroll
+    for (int j = 0; j < PAIRS; ++j) {
+        const f2 cpd = fadd2(C[j], Sn[j]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            acc[j][3 * k] = ffma2(o[3 * k], cpd, acc[j][3 * k]);
+            acc[j][3 * k + 1] = ffma2(o[3 * k + 1], Sn[j], acc[j][3 * k + 1]);
+            acc[j][3 * k + 2] = ffma2(o[3 * k + 2], C[j], acc[j][3 * k + 2]);
+        }
+    }
+}
+
 // P += V * (cos + i sin) for every pixel pair: re += vr c - vi s ; im += vr s + vi c
 template <int PAIRS>
 __device__ __forceinline__ void channel_macs(f2 (&acc)[PAIRS][8], const float4 *vv, const f2 (&C)[PAIRS],
@@ -128,13 +154,19 @@ __device__ __forceinline__ void channel_macs(f2 (&acc)[PAIRS][8], const float4 *
     }
 }
 
+// Kernel variant bits (the PIPE template argument).
+constexpr int kPipe = 1;     // software-pipelined channel loop
+constexpr int kFtz = 2;      // SFU sine/cosine flushing subnormal arguments
+constexpr int kGauss = 4;    // three-multiplication MACs (12 accumulators per pair)
+constexpr int kUnroll2 = 8;  // channel loop unrolled by two
+
 // One staged tile: tt timesteps x ncc channels.
-// PIPE = 1: the channel loop is software pipelined -- the sincos of channel c+1
-// is issued before the MACs of channel c, so a warp keeps SFU and FMA work in
-// flight together (more registers).  PIPE & 1 = 0: phasors then MACs per
-// channel.  PIPE & 2: SFU sine/cosine with subnormal flushing.
-template <int PAIRS, bool FAST, int PIPE>
-__device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[PAIRS], const float4 *coef,
+// PIPE & kPipe: the channel loop is software pipelined -- the sincos of channel
+// c+1 is issued before the MACs of channel c, so a warp keeps SFU and FMA work
+// in flight together (more registers).  Otherwise phasors then MACs per channel.
+// NACC = 8 (four complex MACs) or 12 (Gauss form); UNR = channel-loop unrolling.
+template <int PAIRS, bool FAST, int PIPE, int NACC, int UNR>
+__device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][NACC], const int (&pr)[PAIRS], const float4 *coef,
                                           const f2 *geo, const float4 *vexp, const f2 *kp, int tt, int ncc) {
     for (int t = 0; t < tt; ++t) {
         const float4 c0 = coef[3 * t], c1 = coef[3 * t + 1], c2 = coef[3 * t + 2];
@@ -148,11 +180,11 @@ __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[P
             Q[j] = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
         }
         const float4 *vt = vexp + (size_t)t * ncc * 6;
-        constexpr bool FTZ = (PIPE & 2) != 0;
-        if (PIPE & 1) {
+        constexpr bool FTZ = (PIPE & kFtz) != 0;
+        if (PIPE & kPipe) {
             f2 Cn[PAIRS], Sn[PAIRS];
             channel_phasors<PAIRS, FAST, FTZ>(kp[0], tau0, Q, Cn, Sn);
-#pragma unroll 1
+#pragma unroll UNR
             for (int c = 0; c + 1 < ncc; ++c) {
                 f2 C[PAIRS], S[PAIRS];
 #pragma unroll
@@ -165,7 +197,7 @@ __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[P
             }
             channel_macs<PAIRS>(acc, vt + 6 * (ncc - 1), Cn, Sn);
         } else {
-#pragma unroll 1
+#pragma unroll UNR
             for (int c = 0; c < ncc; ++c) {
                 f2 C[PAIRS], S[PAIRS];
                 channel_phasors<PAIRS, FAST, FTZ>(kp[c], tau0, Q, C, S);
@@ -180,6 +212,8 @@ __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][8], const int (&pr)[P
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
     constexpr int kT = NT, kPairs = PAIRS, kPassPairs = NT * PAIRS, kTileVis = TV, kMaxChunk = TV;
+    constexpr bool kG = (PIPE & kGauss) != 0;
+    constexpr int kAcc = kG ? 12 : 8, kUnr = (PIPE & kUnroll2) ? 2 : 1;
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = a.S, S2 = S * S, npairs = S2 / 2;
     const Layout L = layout(S, a.C, TV);
@@ -247,11 +281,11 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
         const float nmax = gc.z;
 
         for (int pass = 0; pass * kPassPairs < npairs; ++pass) {
-            f2 acc[kPairs][8];
+            f2 acc[kPairs][kAcc];
 #pragma unroll
             for (int j = 0; j < kPairs; ++j)
 #pragma unroll
-                for (int r = 0; r < 8; ++r) acc[j][r] = 0ull;
+                for (int r = 0; r < kAcc; ++r) acc[j][r] = 0ull;
             int pr[kPairs];
 #pragma unroll
             for (int j = 0; j < kPairs; ++j) {
@@ -305,12 +339,26 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
                     for (int i = tid; i < tt * ncc; i += kT) {
                         const float4 v0 = raw[2 * i], v1 = raw[2 * i + 1];
                         float4 *d = vexp + 6 * i;
-                        d[0] = make_float4(v0.x, v0.x, v0.y, v0.y);
-                        d[1] = make_float4(v0.z, v0.z, v0.w, v0.w);
-                        d[2] = make_float4(v1.x, v1.x, v1.y, v1.y);
-                        d[3] = make_float4(v1.z, v1.z, v1.w, v1.w);
-                        d[4] = make_float4(-v0.y, -v0.y, -v0.w, -v0.w);
-                        d[5] = make_float4(-v1.y, -v1.y, -v1.w, -v1.w);
+                        if (kG) {
+                            // per correlation: a, a + b, b - a (each duplicated)
+                            const float re[4] = {v0.x, v0.z, v1.x, v1.z}, im[4] = {v0.y, v0.w, v1.y, v1.w};
+                            float e[12];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) {
+                                e[3 * k] = re[k];
+                                e[3 * k + 1] = re[k] + im[k];
+                                e[3 * k + 2] = im[k] - re[k];
+                            }
+#pragma unroll
+                            for (int q = 0; q < 6; ++q) d[q] = make_float4(e[2 * q], e[2 * q], e[2 * q + 1], e[2 * q + 1]);
+                        } else {
+                            d[0] = make_float4(v0.x, v0.x, v0.y, v0.y);
+                            d[1] = make_float4(v0.z, v0.z, v0.w, v0.w);
+                            d[2] = make_float4(v1.x, v1.x, v1.y, v1.y);
+                            d[3] = make_float4(v1.z, v1.z, v1.w, v1.w);
+                            d[4] = make_float4(-v0.y, -v0.y, -v0.w, -v0.w);
+                            d[5] = make_float4(-v1.y, -v1.y, -v1.w, -v1.w);
+                        }
                     }
                     if (tid == 0) {
                         head->fast = (3.1416f + kappa_max * __int_as_float(head->qmax_bits)) <= kFastBound ? 1 : 0;
@@ -321,9 +369,9 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 
                     // ---- compute
                     if (fast)
-                        grid_tile<kPairs, true, PIPE>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
+                        grid_tile<kPairs, true, PIPE, kAcc, kUnr>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
                     else
-                        grid_tile<kPairs, false, PIPE>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
+                        grid_tile<kPairs, false, PIPE, kAcc, kUnr>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
                 }
                 if (head->abort) break;
             }
@@ -342,8 +390,14 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 #pragma unroll
                 for (int pol = 0; pol < 4; ++pol) {
                     float r0, r1, i0, i1;
-                    unpack2(acc[j][2 * pol], r0, r1);
-                    unpack2(acc[j][2 * pol + 1], i0, i1);
+                    if (kG) {
+                        // Re = k1 - k2, Im = k1 + k3
+                        unpack2(fsub2(acc[j][3 * pol], acc[j][3 * pol + 1]), r0, r1);
+                        unpack2(fadd2(acc[j][3 * pol], acc[j][3 * pol + 2]), i0, i1);
+                    } else {
+                        unpack2(acc[j][2 * pol], r0, r1);
+                        unpack2(acc[j][2 * pol + 1], i0, i1);
+                    }
                     px[0][pol] = {r0, i0};
                     px[1][pol] = {r1, i1};
                 }
@@ -381,6 +435,10 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 //   4: 128 x 2, 128-visibility tiles, 4 CTAs/SM (16 warps), plain channel loop
 //   5: shape 0 with the subnormal-flushing SFU sine/cosine
 //   6: shape 1 with the subnormal-flushing SFU sine/cosine
+//   7: 128 x 4, 2 CTAs/SM, Gauss MACs, channel loop unrolled by two
+//   8: 128 x 4, 2 CTAs/SM, Gauss MACs, pipelined and unrolled by two
+//   9: 256 x 2, 2 CTAs/SM (16 warps), Gauss MACs, unrolled by two
+//  10: 128 x 4, 3 CTAs/SM, Gauss MACs
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -402,7 +460,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return 7; }
+int gridder_fast_shapes() { return 11; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -412,6 +470,10 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 4: return launch_shape<128, 2, 128, 4, 0>(a, stream);
     case 5: return launch_shape<128, 4, 256, 3, 2>(a, stream);
     case 6: return launch_shape<128, 4, 256, 2, 3>(a, stream);
+    case 7: return launch_shape<128, 4, 256, 2, kGauss | kUnroll2>(a, stream);
+    case 8: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll2>(a, stream);
+    case 9: return launch_shape<256, 2, 256, 2, kGauss | kUnroll2>(a, stream);
+    case 10: return launch_shape<128, 4, 256, 3, kGauss>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }

@@ -61,6 +61,11 @@ __device__ __forceinline__ float cos_ftz(float x) {
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
+// Two packed pairs from shared memory in one 16-byte load, straight into the
+// 64-bit registers the packed instructions read (no repacking moves).
+__device__ __forceinline__ void lds2(uint32_t addr, f2 &a, f2 &b) {
+    asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(addr));
+}
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
