@@ -20,6 +20,9 @@ Printed (rank 0, one JSON line):
           top-level figures are those of the kernel with the larger time share
   cpu_baseline the reference's CPU algorithm (the oracle's float restatement of
           its OpenMP launchers) on a bounded sample of the same workload
+  serving p50 / p99 job latency and Mvis/s of a Poisson stream of gridding and
+          degridding jobs of mixed sizes (16-200 stations, 64-2048 timesteps,
+          8-64 channels, 1024^2-8192^2 grids) served with continuous batching
 
 --impl reference times that CPU implementation alone (rank 0) on the same
 workload and metric.
@@ -62,6 +65,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of each baseline half")
     ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline (profiling runs)")
     ap.add_argument("--max-subgrids", type=int, default=0, help="use only the first N subgrids of the plan (profiling)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving (p50/p99 latency) leg")
+    ap.add_argument("--serve-jobs", type=int, default=10, help="observations in the serving leg (2 jobs each)")
+    ap.add_argument("--serve-rate", type=float, default=16.0, help="mean arrival rate of the serving leg, jobs/s")
     ap.add_argument("--shapes", default="", help="G,D: batched gridder/degridder launch shapes instead of autotuning")
     return ap.parse_args()
 
@@ -339,8 +345,8 @@ def run_ours(args, rank, world, local_rank):
         "traffic": per_kernel[dom]["traffic"],
         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the first 8192 "
                           "subgrids of this plan, scaled by subgrids (the kernels stream each subgrid's data once)",
-        "peak_source": "measured in this run: FFMA microbenchmark idg_measure_fp32_peak (MEASURED_PEAKS.json "
-                       "holds HBM and bf16 figures only); the SFU bound (16 sin/cos per SM clock, 2 per "
+        "peak_source": "measured in this run: FFMA microbenchmark idg_measure_fp32_peak (no FP32 FMA figure "
+                       "is provided by MEASURED_PEAKS.json); the SFU bound (16 sin/cos per SM clock, 2 per "
                        "pixel-visibility) is within 2% of the FMA bound on GB300",
         "algorithmic": "34 flop (17 FMA) + 1 sincos per pixel-visibility; %.3g pixel-visibilities per launch" % pixvis,
         "gridder": per_kernel["gridder"],
@@ -398,6 +404,16 @@ def run_ours(args, rank, world, local_rank):
         ops.release_buffers()
         del out_host
 
+    # serving: a Poisson stream of gridding and degridding jobs of mixed sizes
+    serving = None
+    if not args.no_serve:
+        from idg_gb300 import serve_bench
+
+        srng = np.random.default_rng(5 + rank)
+        jobs = [serve_bench.make_observation(srng, 2e7) for _ in range(args.serve_jobs)]
+        serving = serve_bench.run_stream(jobs, args.serve_rate, slots=4, budget_gb=64.0, seed=5 + rank)
+        del jobs
+
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(obs, vis_host.numpy() if vis_host is not None else None, args.cpu_seconds)
 
@@ -426,6 +442,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roof,
         "cpu_baseline": cpu,
         "plain": plain,
+        "serving": serving,
         "clocks": clock_info,
     }
 

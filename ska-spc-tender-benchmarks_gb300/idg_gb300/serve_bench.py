@@ -51,6 +51,41 @@ def make_observation(rng, max_vis: float):
     return spec, grid_job, degrid_job
 
 
+def run_stream(observations, rate: float, slots: int = 4, budget_gb: float = 96.0, seed: int = 5) -> dict:
+    """Serve the gridding and degridding jobs of `observations` as one Poisson
+    stream of mean rate `rate` jobs/s; returns the latency / throughput line."""
+    with Server(max_slots=slots, hbm_budget_bytes=int(budget_gb * (1 << 30)), cta_share=True) as srv:
+        grids = [srv.grid_create(spec.grid_size) for spec, _, _ in observations]
+        # a random interleaving in which each observation's gridding job precedes its degridding job
+        order = np.random.default_rng(seed + 1).permutation(2 * len(observations)).reshape(-1, 2)
+        events = []
+        for i, (p, q) in enumerate(order):
+            events.append((min(p, q), (_lib.IDG_JOB_GRID, observations[i][1], grids[i])))
+            events.append((max(p, q), (_lib.IDG_JOB_DEGRID, observations[i][2], grids[i])))
+        stream = [job for _, job in sorted(events, key=lambda e: e[0])]
+        st = poisson_load(srv, stream, rate, seed=seed)
+        for g in grids:
+            srv.grid_release(g)
+    lat = sorted(j["latency_ms"] for j in st["jobs"])
+    return {
+        "metric": "serving: job latency and throughput, Poisson arrivals",
+        "rate_jobs_per_s": rate,
+        "jobs": len(stream),
+        "completed": st["completed"],
+        "rejected": st["rejected"],
+        "p50_ms": st["p50_ms"],
+        "p99_ms": st["p99_ms"],
+        "mean_ms": st["mean_ms"],
+        "max_ms": lat[-1] if lat else None,
+        "mvis_per_s": st["mvis_per_s"],
+        "hbm_peak_gb": st["hbm_peak"] / 1e9,
+        "slots": slots,
+        "budget_gb": budget_gb,
+        "visibilities": int(sum(j["visibilities"] for j in st["jobs"])),
+        "wall_s": st["wall_s"],
+    }
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--rates", default="2,4,8")
@@ -65,38 +100,9 @@ def main(argv=None):
     observations = [make_observation(rng, args.max_vis) for _ in range(args.jobs)]
     results = []
     for rate in [float(r) for r in args.rates.split(",")]:
-        with Server(max_slots=args.slots, hbm_budget_bytes=int(args.budget_gb * (1 << 30)), cta_share=True) as srv:
-            grids = [srv.grid_create(spec.grid_size) for spec, _, _ in observations]
-            # a random interleaving in which each observation's gridding job precedes its degridding job
-            slots = np.random.default_rng(args.seed + 1).permutation(2 * len(observations)).reshape(-1, 2)
-            events = []
-            for i, (p, q) in enumerate(slots):
-                events.append((min(p, q), (_lib.IDG_JOB_GRID, observations[i][1], grids[i])))
-                events.append((max(p, q), (_lib.IDG_JOB_DEGRID, observations[i][2], grids[i])))
-            stream = [job for _, job in sorted(events, key=lambda e: e[0])]
-            st = poisson_load(srv, stream, rate, seed=args.seed)
-            lat = sorted(j["latency_ms"] for j in st["jobs"])
-            line = {
-                "metric": "serving: job latency and throughput, Poisson arrivals",
-                "rate_jobs_per_s": rate,
-                "jobs": len(stream),
-                "completed": st["completed"],
-                "rejected": st["rejected"],
-                "p50_ms": st["p50_ms"],
-                "p99_ms": st["p99_ms"],
-                "mean_ms": st["mean_ms"],
-                "max_ms": lat[-1] if lat else None,
-                "mvis_per_s": st["mvis_per_s"],
-                "hbm_peak_gb": st["hbm_peak"] / 1e9,
-                "slots": args.slots,
-                "budget_gb": args.budget_gb,
-                "visibilities": int(sum(j["visibilities"] for j in st["jobs"])),
-                "wall_s": st["wall_s"],
-            }
-            print(json.dumps(line), flush=True)
-            results.append(line)
-            for g in grids:
-                srv.grid_release(g)
+        line = run_stream(observations, rate, args.slots, args.budget_gb, args.seed)
+        print(json.dumps(line), flush=True)
+        results.append(line)
     return results
 
 
