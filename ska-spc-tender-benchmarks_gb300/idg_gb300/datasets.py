@@ -125,6 +125,7 @@ class Observation:
     aterms: np.ndarray       # [slots, ns, S, S, 4] complex64
     taper: np.ndarray        # [S, S] float32
     metadata: np.ndarray     # [N] METADATA_DTYPE
+    ext: np.ndarray | None = None  # [N] SUBGRID_EXT_DTYPE channel ranges (split plans only)
 
 
 def stations_in_disk(n: int, radius: float, rng: np.random.Generator) -> np.ndarray:
@@ -194,6 +195,99 @@ def plan_subgrids(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.ndarra
     return md
 
 
+def plan_subgrids_split(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.ndarray, baselines: np.ndarray,
+                        margin: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+    """uvw-driven plan with channel and time splitting, for baselines whose
+    uv track over all channels and ``timesteps_per_subgrid`` steps does not
+    fit one subgrid.
+
+    Per baseline, the channels are cut into contiguous groups whose spread in
+    frequency alone covers at most half the usable width (S - margin cells) at
+    the baseline's longest |u| or |v|; per channel group the time axis is then
+    walked and a subgrid closed when the uv extent of its visibilities (all its
+    channels, all its timesteps) would exceed S - margin cells, when it holds
+    ``timesteps_per_subgrid`` steps, or at an A-term slot boundary.  The corner
+    is placed as in ``plan_subgrids`` (centre cell on the centre of the extent).
+    Returns (metadata METADATA_DTYPE[N], ext SUBGRID_EXT_DTYPE[N] with the
+    channel range [channel_begin, channel_end) of each subgrid).  Every
+    (baseline, timestep, channel) sample belongs to exactly one subgrid."""
+    from ._lib import SUBGRID_EXT_DTYPE
+
+    nb, nt = spec.n_baselines, spec.ntimesteps
+    S, G, img = spec.subgrid_size, spec.grid_size, spec.image_size
+    width = S - (S // 4 if margin is None else margin)
+    tmax = spec.timesteps_per_subgrid
+    f = np.asarray(frequencies, np.float64)
+    scale = img / SPEED_OF_LIGHT  # cells per (metre * Hz)
+    rows_md, rows_ext = [], []
+    for b in range(nb):
+        u = uvw[b * nt:(b + 1) * nt, 0].astype(np.float64)
+        v = uvw[b * nt:(b + 1) * nt, 1].astype(np.float64)
+        reach = max(np.abs(u).max(), np.abs(v).max()) * scale
+        # channel groups
+        groups, c0 = [], 0
+        for c in range(1, len(f) + 1):
+            if c == len(f) or reach * (f[c] - f[c0]) > 0.5 * width:
+                groups.append((c0, c))
+                c0 = c
+        for c0, c1 in groups:
+            fa, fb = f[c0], f[c1 - 1]
+            ua, ub, va, vb = u * fa * scale, u * fb * scale, v * fa * scale, v * fb * scale
+            lo_u, hi_u = np.minimum(ua, ub), np.maximum(ua, ub)
+            lo_v, hi_v = np.minimum(va, vb), np.maximum(va, vb)
+            t0 = 0
+            while t0 < nt:
+                t1 = min(nt, t0 + tmax)
+                if spec.aterm_interval > 0:
+                    t1 = min(t1, (t0 // spec.aterm_interval + 1) * spec.aterm_interval)
+                seg = slice(t0, t1)
+                ext_u = np.maximum.accumulate(hi_u[seg]) - np.minimum.accumulate(lo_u[seg])
+                ext_v = np.maximum.accumulate(hi_v[seg]) - np.minimum.accumulate(lo_v[seg])
+                fits = np.nonzero(np.maximum(ext_u, ext_v) > width)[0]
+                n = int(fits[0]) if fits.size else t1 - t0
+                n = max(n, 1)
+                s = slice(t0, t0 + n)
+                mid_u = 0.5 * (lo_u[s].min() + hi_u[s].max())
+                mid_v = 0.5 * (lo_v[s].min() + hi_v[s].max())
+                rows_md.append((0, b * nt + t0, n, t0 // spec.aterm_interval if spec.aterm_interval > 0 else 0,
+                                baselines[b, 0], baselines[b, 1],
+                                int(np.floor(mid_u + G / 2 - S / 2 + 0.5)), int(np.floor(mid_v + G / 2 - S / 2 + 0.5)),
+                                0))
+                rows_ext.append((c0, c1))
+                t0 += n
+    md = np.array(rows_md, dtype=METADATA_DTYPE)
+    ext = np.array(rows_ext, dtype=SUBGRID_EXT_DTYPE)
+    return md, ext
+
+
+def subgrid_uv_extent(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.ndarray, md: np.ndarray,
+                      ext: np.ndarray) -> np.ndarray:
+    """Per subgrid of a split plan, the larger of its u and v extents in grid cells."""
+    f = np.asarray(frequencies, np.float64)
+    scale = spec.image_size / SPEED_OF_LIGHT
+    out = np.empty(md.shape[0])
+    for i, (m, e) in enumerate(zip(md, ext)):
+        r = slice(int(m["time_offset"]), int(m["time_offset"]) + int(m["nr_timesteps"]))
+        fr = f[int(e["channel_begin"]):int(e["channel_end"])]
+        w = []
+        for k in (0, 1):
+            a = uvw[r, k].astype(np.float64)[:, None] * fr[None, :] * scale
+            w.append(a.max() - a.min())
+        out[i] = max(w)
+    return out
+
+
+def config3(subgrid_size: int = 32, nstations: int = 100, ntimesteps: int = 8192, seed: int = 3) -> ObservationSpec:
+    """The precision-sweep generator: config 2's with baselines to 100 km, 64 channels
+    100-200 MHz, subgrids of 32^2 or 64^2, an 8192^2 grid (long baselines reach
+    +-3,300 cells at 200 MHz) and at most 128 timesteps per subgrid; planned with
+    ``plan_subgrids_split``.  ``nstations`` / ``ntimesteps`` shrink it for tests."""
+    return ObservationSpec(nstations=nstations, disk_radius_m=50000.0, ntimesteps=ntimesteps,
+                           timesteps_per_subgrid=128, nchannels=64, f_start=100e6, f_end=200e6,
+                           subgrid_size=subgrid_size, grid_size=8192, image_size=0.05, aterm_sigma=0.05,
+                           aterm_interval=256, seed=seed)
+
+
 def uv_extent_pixels(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.ndarray) -> np.ndarray:
     """Per subgrid, the larger of its u and v extents in grid cells (must stay below S minus the taper support)."""
     nb, nt, T = spec.n_baselines, spec.ntimesteps, spec.timesteps_per_subgrid
@@ -208,7 +302,9 @@ def uv_extent_pixels(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.nda
     return np.maximum(ext[0], ext[1]).reshape(-1)
 
 
-def make_observation(spec: ObservationSpec) -> Observation:
+def make_observation(spec: ObservationSpec, split: bool = False) -> Observation:
+    """Stations, uvw, wavenumbers, A-terms, taper and the plan of `spec`;
+    split=True plans with channel and time splitting (``plan_subgrids_split``)."""
     rng = np.random.default_rng(spec.seed)
     st = stations_in_disk(spec.nstations, spec.disk_radius_m, rng)
     bl = baseline_pairs(spec.nstations)
@@ -226,6 +322,9 @@ def make_observation(spec: ObservationSpec) -> Observation:
         noise = rng.standard_normal((*at.shape, 2), dtype=np.float32)
         at += (spec.aterm_sigma * (noise[..., 0] + 1j * noise[..., 1])).astype(np.complex64)
     taper = pswf_taper(S, spec.taper_c)
+    if split:
+        md, ext = plan_subgrids_split(spec, uvw, freqs, bl)
+        return Observation(spec, st, bl, uvw, freqs, k, at, taper, md, ext)
     md = plan_subgrids(spec, uvw, freqs, bl)
     return Observation(spec, st, bl, uvw, freqs, k, at, taper, md)
 

@@ -1,0 +1,86 @@
+"""Precision sweep on the config-3 generator: baselines to 100 km, 64 channels
+over 100-200 MHz, subgrids of 32^2 and 64^2, planned with channel and time
+splitting (datasets.plan_subgrids_split).
+
+For a seeded sample of subgrids from every baseline-length decile, the
+gridder's subgrids and the degridder's visibilities of both variants are
+compared with the FP64 oracle of the same gridder/degridder.  Relative RMS and
+maximum error (max |got - want| over the RMS of want) are printed per decile as
+one JSON line each, and the relative RMS is held to the 1e-5 tolerance overall
+and in every decile.  The observation is the config-3 generator shrunk to 12
+stations and 512 timesteps so that the FP64 oracle finishes in seconds.
+"""
+import json
+
+import numpy as np
+import pytest
+
+import idg_gb300._lib as L
+from gpu_helpers import degrid_gpu, grid_gpu, spec_for
+from test_gpu_kernels import _oracle_with_ext
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+PER_DECILE = 16
+
+
+def _decile_errors(got, want, decile, nd=10):
+    out = []
+    for d in range(nd):
+        sel = decile == d
+        if not np.any(sel):
+            continue
+        g, w = got[sel], want[sel]
+        scale = np.sqrt(np.mean(np.abs(w) ** 2))
+        out.append({"decile": d, "rel_rms": float(np.linalg.norm(g - w) / np.linalg.norm(w)),
+                    "max_err": float(np.abs(g - w).max() / scale)})
+    return out
+
+
+@pytest.mark.parametrize("S", [32, 64])
+def test_precision_sweep_by_baseline_decile(oracle_mod, idg, S):
+    from idg_gb300 import datasets as D
+
+    spec = D.config3(S, nstations=12, ntimesteps=512)
+    obs = D.make_observation(spec, split=True)
+    md_all, ext_all = obs.metadata, obs.ext
+    C = spec.nchannels
+    # baseline length of every subgrid, deciles over subgrids
+    enu = obs.stations[obs.baselines[:, 1]] - obs.stations[obs.baselines[:, 0]]
+    blen = np.linalg.norm(enu, axis=1)
+    sub_bl = md_all["time_offset"] // spec.ntimesteps
+    edges = np.quantile(blen[sub_bl], np.linspace(0, 1, 11)[1:-1])
+    dec_all = np.searchsorted(edges, blen[sub_bl], side="right")
+    rng = np.random.default_rng(7 + S)
+    pick = np.sort(np.concatenate([rng.choice(np.where(dec_all == d)[0], min(PER_DECILE, int((dec_all == d).sum())),
+                                              replace=False) for d in range(10)]))
+    md, ext, dec = md_all[pick].copy(), ext_all[pick].copy(), dec_all[pick]
+    N = md.shape[0]
+    rows = obs.uvw.shape[0]
+    vis = (rng.standard_normal((rows, C, 4)) + 1j * rng.standard_normal((rows, C, 4))).astype(np.complex64)
+    sub_in = (rng.standard_normal((N, 4, S, S)) + 1j * rng.standard_normal((N, 4, S, S))).astype(np.complex64)
+    want_g, want_v = _oracle_with_ext(oracle_mod, spec.grid_size, S, spec.nstations, spec.image_size, obs.uvw,
+                                      obs.wavenumbers, vis, obs.taper, obs.aterms, md, ext, sub_in)
+    covered = np.zeros((rows, C), bool)
+    vdec = np.full((rows, C), -1)
+    for m, e, d in zip(md, ext, dec):
+        r = slice(int(m["time_offset"]), int(m["time_offset"]) + int(m["nr_timesteps"]))
+        covered[r, e["channel_begin"]:e["channel_end"]] = True
+        vdec[r, e["channel_begin"]:e["channel_end"]] = d
+    sp = spec_for(spec.grid_size, S, C, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    for variant in (L.VARIANT_PLAIN, L.VARIANT_BATCHED):
+        got_g = grid_gpu(sp, md, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, variant, ext=ext)
+        got_v = degrid_gpu(sp, md, obs.uvw, obs.wavenumbers, sub_in, obs.taper, obs.aterms, rows, variant, ext=ext)
+        gd = _decile_errors(got_g.reshape(N, -1), want_g.reshape(N, -1), dec)
+        vd = _decile_errors(got_v[covered], want_v[covered], vdec[covered])
+        overall_g = float(np.linalg.norm(got_g - want_g) / np.linalg.norm(want_g))
+        overall_v = float(np.linalg.norm(got_v[covered] - want_v[covered]) / np.linalg.norm(want_v[covered]))
+        for name, table, overall in (("grid", gd, overall_g), ("vis", vd, overall_v)):
+            line = {"S": S, "variant": "batched" if variant == L.VARIANT_BATCHED else "plain", "output": name,
+                    "subgrids": int(N), "overall_rel_rms": overall,
+                    "baseline_decile_edges_km": [round(float(x) / 1e3, 1) for x in edges], "deciles": table}
+            print("[precision] " + json.dumps(line))
+            assert overall <= TOL, line
+            assert max(t["rel_rms"] for t in table) <= TOL, line
+        assert np.all(got_v[~covered] == 0)

@@ -130,3 +130,30 @@ def test_plan_is_deterministic(idg):
     b = D.make_observation(D.config1())
     assert np.array_equal(a.metadata.view(np.uint8), b.metadata.view(np.uint8))
     assert np.array_equal(a.uvw, b.uvw)
+
+
+@pytest.mark.parametrize("S", [32, 64])
+def test_split_plan_covers_every_sample_once_and_fits(idg, S):
+    """The channel/time-splitting planner (long baselines, wide bands): every
+    (baseline, timestep, channel) sample in exactly one subgrid, every subgrid's
+    uv extent within S - S/4 cells, subgrids inside the grid, no subgrid across
+    an A-term slot boundary, and the same plan from the same seed."""
+    from idg_gb300 import datasets as D
+
+    spec = D.config3(S, nstations=8, ntimesteps=512)
+    obs = D.make_observation(spec, split=True)
+    md, ext = obs.metadata, obs.ext
+    assert md.shape == ext.shape and md.shape[0] > spec.n_baselines * (spec.ntimesteps // spec.timesteps_per_subgrid)
+    count = np.zeros((obs.uvw.shape[0], spec.nchannels), np.int32)
+    for m, e in zip(md, ext):
+        count[m["time_offset"]:m["time_offset"] + m["nr_timesteps"], e["channel_begin"]:e["channel_end"]] += 1
+    assert np.all(count == 1)
+    assert D.subgrid_uv_extent(spec, obs.uvw, obs.frequencies, md, ext).max() <= S - S // 4
+    G = spec.grid_size
+    assert (md["x"] >= 0).all() and (md["x"] + S <= G).all() and (md["y"] >= 0).all() and (md["y"] + S <= G).all()
+    t_in_bl = md["time_offset"] % spec.ntimesteps
+    assert np.all(t_in_bl // spec.aterm_interval == (t_in_bl + md["nr_timesteps"] - 1) // spec.aterm_interval)
+    assert np.all(md["aterm_index"] == t_in_bl // spec.aterm_interval)
+    assert np.all(md["nr_timesteps"] <= spec.timesteps_per_subgrid)
+    again = D.make_observation(spec, split=True)
+    assert np.array_equal(again.metadata, md) and np.array_equal(again.ext, ext)
