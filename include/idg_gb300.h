@@ -218,6 +218,23 @@ IDG_API int idg_plan_launch_cycle(idg_plan *plan, void *stream);
 /* Reads (and optionally clears) the plan's device check word; synchronises `stream`. */
 IDG_API int idg_plan_status(idg_plan *plan, void *stream, uint32_t *status, int clear);
 
+/* One imaging cycle over several plans that share one uv-grid -- typically one
+ * plan per subgrid size of a job whose subgrids differ in size -- captured as a
+ * single CUDA graph: zero `grid`, the gridding step of every plan in order,
+ * then the degridding step of every plan.  Plans may differ in subgrid size and
+ * channel count but must agree on grid_size and nr_w_planes.  Array arguments
+ * hold one DEVICE pointer per plan (plan i reads uvw[i], wavenumbers[i],
+ * visibilities_in[i], spheroidal[i], aterms[i] and writes visibilities_out[i]).
+ * The buffers must stay allocated while the cycle is used.  No counterpart in
+ * the reference. */
+typedef struct idg_cycle idg_cycle;
+IDG_API int idg_cycle_capture(int nr_plans, idg_plan *const *plans, const float *const *uvw,
+                              const float *const *wavenumbers, const void *const *visibilities_in,
+                              const float *const *spheroidal, const void *const *aterms, void *grid,
+                              void *const *visibilities_out, idg_cycle **cycle);
+IDG_API int idg_cycle_launch(idg_cycle *cycle, void *stream);
+IDG_API int idg_cycle_destroy(idg_cycle *cycle);
+
 /* ------------------------------------------------------------------ */
 /* Serving: continuous batching of gridding / degridding jobs          */
 /* ------------------------------------------------------------------ */

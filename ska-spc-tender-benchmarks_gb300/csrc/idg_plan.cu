@@ -32,6 +32,12 @@ struct idg_plan {
     cudaGraphExec_t graph_exec = nullptr;
 };
 
+// A captured cycle over several plans sharing one grid (idg_cycle_capture).
+struct idg_cycle {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+};
+
 namespace {
 
 using namespace idg;
@@ -251,6 +257,73 @@ IDG_API int idg_plan_capture_cycle(idg_plan *plan, const float *uvw, const float
 IDG_API int idg_plan_launch_cycle(idg_plan *plan, void *stream) {
     if (!plan || !plan->graph_exec) return fail(IDG_ERR_INVALID_ARGUMENT, "plan has no captured cycle");
     IDG_CUDA(cudaGraphLaunch(plan->graph_exec, reinterpret_cast<cudaStream_t>(stream)));
+    return IDG_OK;
+}
+
+IDG_API int idg_cycle_capture(int nr_plans, idg_plan *const *plans, const float *const *uvw,
+                              const float *const *wavenumbers, const void *const *visibilities_in,
+                              const float *const *spheroidal, const void *const *aterms, void *grid,
+                              void *const *visibilities_out, idg_cycle **cycle) {
+    if (!cycle) return fail(IDG_ERR_INVALID_ARGUMENT, "cycle output is NULL");
+    *cycle = nullptr;
+    if (nr_plans < 1 || !plans || !uvw || !wavenumbers || !visibilities_in || !spheroidal || !aterms ||
+        !visibilities_out)
+        return fail(IDG_ERR_INVALID_ARGUMENT, "nr_plans %d or a NULL array", nr_plans);
+    const idg_params &q0 = plans[0] ? plans[0]->params : idg_params{};
+    for (int i = 0; i < nr_plans; ++i) {
+        idg_plan *p = plans[i];
+        if (!p) return fail(IDG_ERR_INVALID_ARGUMENT, "plan %d is NULL", i);
+        if (p->params.grid_size != q0.grid_size || p->params.nr_w_planes != q0.nr_w_planes)
+            return fail(IDG_ERR_INVALID_ARGUMENT, "plan %d: grid %d x %d planes differs from plan 0 (%d x %d)", i,
+                        p->params.grid_size, p->params.nr_w_planes, q0.grid_size, q0.nr_w_planes);
+        if (int rc = check_data(p, uvw[i], wavenumbers[i], visibilities_in[i], spheroidal[i], aterms[i], grid))
+            return rc;
+        if (!visibilities_out[i] || !aligned16(visibilities_out[i]))
+            return fail(IDG_ERR_INVALID_ARGUMENT, "visibilities_out[%d] must be a 16-byte aligned device pointer", i);
+    }
+    auto *c = new idg_cycle();
+    const size_t b_grid = (size_t)(q0.nr_w_planes > 0 ? q0.nr_w_planes : 1) * 4 * q0.grid_size * q0.grid_size * 8;
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "stream for the cycle capture");
+    }
+    int rc = IDG_OK;
+    e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        e = cudaMemsetAsync(grid, 0, b_grid, st);
+        for (int i = 0; e == cudaSuccess && !rc && i < nr_plans; ++i)
+            rc = grid_step(plans[i], uvw[i], wavenumbers[i], visibilities_in[i], spheroidal[i], aterms[i], grid, st);
+        for (int i = 0; e == cudaSuccess && !rc && i < nr_plans; ++i)
+            rc = degrid_step(plans[i], uvw[i], wavenumbers[i], visibilities_out[i], spheroidal[i], aterms[i], grid, st);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(st, &g);
+        if (e == cudaSuccess) e = e2;
+        c->graph = g;
+    }
+    cudaStreamDestroy(st);
+    if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&c->graph_exec, c->graph, 0);
+    if (rc || e != cudaSuccess) {
+        if (c->graph) cudaGraphDestroy(c->graph);
+        delete c;
+        return rc ? rc : cuda_fail(e, "graph capture of the multi-plan cycle");
+    }
+    *cycle = c;
+    return IDG_OK;
+}
+
+IDG_API int idg_cycle_launch(idg_cycle *cycle, void *stream) {
+    if (!cycle || !cycle->graph_exec) return fail(IDG_ERR_INVALID_ARGUMENT, "cycle is NULL or empty");
+    IDG_CUDA(cudaGraphLaunch(cycle->graph_exec, reinterpret_cast<cudaStream_t>(stream)));
+    return IDG_OK;
+}
+
+IDG_API int idg_cycle_destroy(idg_cycle *cycle) {
+    if (!cycle) return IDG_OK;
+    if (cycle->graph_exec) cudaGraphExecDestroy(cycle->graph_exec);
+    if (cycle->graph) cudaGraphDestroy(cycle->graph);
+    delete cycle;
     return IDG_OK;
 }
 

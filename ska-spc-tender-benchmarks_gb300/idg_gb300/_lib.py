@@ -187,6 +187,10 @@ _SIGNATURES = {
     "idg_plan_capture_cycle": [_P, _P, _P, _P, _P, _P, _P, _P],
     "idg_plan_launch_cycle": [_P, _P],
     "idg_plan_status": [_P, _P, ctypes.POINTER(ctypes.c_uint32), _I32],
+    "idg_cycle_capture": [_I32, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
+                          ctypes.POINTER(_P), ctypes.POINTER(_P), _P, ctypes.POINTER(_P), ctypes.POINTER(_P)],
+    "idg_cycle_launch": [_P, _P],
+    "idg_cycle_destroy": [_P],
     "idg_server_create": [ctypes.POINTER(IdgServerConfig), ctypes.POINTER(ctypes.c_void_p)],
     "idg_server_destroy": [_P],
     "idg_server_grid_create": [_P, _I32, _I32, ctypes.POINTER(ctypes.c_int64)],

@@ -288,6 +288,79 @@ def config3(subgrid_size: int = 32, nstations: int = 100, ntimesteps: int = 8192
                            aterm_interval=256, seed=seed)
 
 
+def config4(n_subgrids: int = 50000, nstations: int = 2000, sizes=(24, 32, 48), groups=(8, 16, 32, 64),
+            seed: int = 4) -> list[Observation]:
+    """The batched-uneven generator: `n_subgrids` subgrids sampled from the
+    baselines of `nstations` stations in a 10 km disk (config-2 geometry), each
+    with its own time window of T timesteps, T log-uniform in [16, 256], starting
+    at a random hour angle within +-4 h; a channel group of 8, 16, 32 or 64 of 64
+    channels over 150-160 MHz (at a random group-aligned offset); a subgrid size
+    drawn from `sizes`; an 8192^2 grid.  A-terms are identity + 0.05 N(0,1), one
+    slot.  Returns one Observation per subgrid size, each with its own uvw rows
+    (a subgrid's rows are contiguous), metadata and channel sidecar; the
+    ObservationSpec of each has ntimesteps = its row count, one "baseline" per
+    row block, and must not be used to re-plan."""
+    from ._lib import SUBGRID_EXT_DTYPE
+
+    rng = np.random.default_rng(seed)
+    st = stations_in_disk(nstations, 5000.0, rng)
+    C, f0, f1, G, img = 64, 150e6, 160e6, 8192, 0.05
+    freqs = np.linspace(f0, f1, C)
+    k = (2 * np.pi * freqs / SPEED_OF_LIGHT).astype(np.float32)
+    s1 = rng.integers(0, nstations - 1, n_subgrids)
+    s2 = s1 + 1 + (rng.random(n_subgrids) * (nstations - 1 - s1)).astype(np.int64)
+    T = np.clip(np.floor(np.exp(rng.uniform(np.log(16), np.log(257), n_subgrids))), 16, 256).astype(np.int64)
+    H0 = rng.uniform(-4, 4, n_subgrids) * 3600 * EARTH_ROTATION_RATE
+    glen = rng.choice(np.asarray(groups), n_subgrids)
+    gofs = np.array([rng.integers(0, C // g) * g for g in glen])
+    size = rng.choice(np.asarray(sizes), n_subgrids)
+    out = []
+    for S in sizes:
+        idx = np.where(size == S)[0]
+        n = idx.size
+        rows = int(T[idx].sum())
+        start = np.concatenate([[0], np.cumsum(T[idx])[:-1]]).astype(np.int64)
+        sub_of_row = np.repeat(np.arange(n), T[idx])
+        t_in = np.arange(rows) - start[sub_of_row]
+        H = H0[idx][sub_of_row] + t_in * EARTH_ROTATION_RATE
+        enu = (st[s2[idx]] - st[s1[idx]])[sub_of_row]
+        lat = dec = np.deg2rad(-30.0)
+        E, N_, U = enu[:, 0], enu[:, 1], enu[:, 2]
+        X = -np.sin(lat) * N_ + np.cos(lat) * U
+        Y, Z = E, np.cos(lat) * N_ + np.sin(lat) * U
+        u = np.sin(H) * X + np.cos(H) * Y
+        v = -np.sin(dec) * np.cos(H) * X + np.sin(dec) * np.sin(H) * Y + np.cos(dec) * Z
+        w = np.cos(dec) * np.cos(H) * X - np.cos(dec) * np.sin(H) * Y + np.sin(dec) * Z
+        uvw = np.stack([u, v, w], axis=1).astype(np.float32)
+        md = np.zeros(n, METADATA_DTYPE)
+        ext = np.zeros(n, SUBGRID_EXT_DTYPE)
+        md["time_offset"] = start
+        md["nr_timesteps"] = T[idx]
+        md["station1"] = s1[idx]
+        md["station2"] = s2[idx]
+        ext["channel_begin"] = gofs[idx]
+        ext["channel_end"] = gofs[idx] + glen[idx]
+        scale = img / SPEED_OF_LIGHT
+        for i in range(n):
+            r = slice(int(start[i]), int(start[i] + T[idx][i]))
+            fa, fb = freqs[gofs[idx][i]], freqs[gofs[idx][i] + glen[idx][i] - 1]
+            uu = np.concatenate([uvw[r, 0] * fa, uvw[r, 0] * fb]) * scale
+            vv = np.concatenate([uvw[r, 1] * fa, uvw[r, 1] * fb]) * scale
+            md["x"][i] = int(np.floor(0.5 * (uu.min() + uu.max()) + G / 2 - S / 2 + 0.5))
+            md["y"][i] = int(np.floor(0.5 * (vv.min() + vv.max()) + G / 2 - S / 2 + 0.5))
+        at = np.zeros((1, nstations, S, S, 4), np.complex64)
+        at[..., 0] = 1
+        at[..., 3] = 1
+        noise = rng.standard_normal((*at.shape, 2), dtype=np.float32)
+        at += (0.05 * (noise[..., 0] + 1j * noise[..., 1])).astype(np.complex64)
+        spec = ObservationSpec(nstations=nstations, disk_radius_m=5000.0, ntimesteps=rows, timesteps_per_subgrid=rows,
+                               nchannels=C, f_start=f0, f_end=f1, subgrid_size=S, grid_size=G, image_size=img,
+                               seed=seed)
+        out.append(Observation(spec, st, np.stack([s1[idx], s2[idx]], 1).astype(np.uint32), uvw, freqs, k, at,
+                               pswf_taper(S, spec.taper_c), md, ext))
+    return out
+
+
 def uv_extent_pixels(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.ndarray) -> np.ndarray:
     """Per subgrid, the larger of its u and v extents in grid cells (must stay below S minus the taper support)."""
     nb, nt, T = spec.n_baselines, spec.ntimesteps, spec.timesteps_per_subgrid

@@ -266,6 +266,43 @@ class Plan:
         return int(v.value)
 
 
+class Cycle:
+    """One imaging cycle over several plans sharing one uv-grid (idg_cycle_*),
+    captured as a single CUDA graph: zero the grid, grid with every plan, then
+    degrid with every plan.  `parts` holds, per plan, the device tensors
+    (uvw, wavenumbers, vis_in, taper, aterms, vis_out)."""
+
+    def __init__(self, plans: list, parts: list, grid):
+        if len(plans) != len(parts) or not plans:
+            raise ValueError("one (uvw, wavenumbers, vis_in, taper, aterms, vis_out) tuple per plan")
+        for p, (uvw, k, vin, taper, at, vout) in zip(plans, parts):
+            p._check(uvw, k, vin, taper, at, grid)
+            _req(vout, "vis_out", torch.complex64, tuple(vin.shape))
+        n = len(plans)
+        arr = lambda xs: (ctypes.c_void_p * n)(*[ptr(x) for x in xs])
+        h = ctypes.c_void_p()
+        _lib.call("idg_cycle_capture", n, (ctypes.c_void_p * n)(*[p._h.value for p in plans]),
+                  arr([q[0] for q in parts]), arr([q[1] for q in parts]), arr([q[2] for q in parts]),
+                  arr([q[3] for q in parts]), arr([q[4] for q in parts]), ptr(grid), arr([q[5] for q in parts]),
+                  ctypes.byref(h))
+        self._h = h
+        self._keep = (plans, parts, grid)  # the graph holds raw addresses
+
+    def launch(self, stream=None) -> None:
+        _lib.call("idg_cycle_launch", self._h, _stream_handle(stream))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().idg_cycle_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def release_buffers() -> None:
     _lib.call("idg_release_buffers")
 
