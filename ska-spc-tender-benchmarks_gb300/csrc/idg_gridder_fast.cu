@@ -439,6 +439,8 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 //   8: 128 x 4, 2 CTAs/SM, Gauss MACs, pipelined and unrolled by two
 //   9: 256 x 2, 2 CTAs/SM (16 warps), Gauss MACs, unrolled by two
 //  10: 128 x 4, 3 CTAs/SM, Gauss MACs
+//  11: 96 x 3 (288 pairs per pass: whole passes for S = 24 and 48), Gauss, pipelined, unrolled by two
+//  12: 128 x 3 (384 pairs per pass: whole passes for S = 48), Gauss, pipelined, unrolled by two
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -460,7 +462,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return 11; }
+int gridder_fast_shapes() { return 13; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -474,6 +476,8 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 8: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll2>(a, stream);
     case 9: return launch_shape<256, 2, 256, 2, kGauss | kUnroll2>(a, stream);
     case 10: return launch_shape<128, 4, 256, 3, kGauss>(a, stream);
+    case 11: return launch_shape<96, 3, 256, 3, kGauss | kPipe | kUnroll2>(a, stream);
+    case 12: return launch_shape<128, 3, 256, 2, kGauss | kPipe | kUnroll2>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }
