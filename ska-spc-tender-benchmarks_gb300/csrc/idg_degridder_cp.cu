@@ -1,0 +1,373 @@
+// idg_degridder_cp.cu -- batched degridder with CHANNEL-pair packing.
+//
+// Same result as idg_degridder.cu / idg_degridder_fast.cu.  The difference is
+// what the two halves of a packed FP32x2 register hold.  The pixel-pair form
+// (idg_degridder_fast.cu) packs two pixels, so every visibility accumulator is
+// a pair of partial sums that is folded at the end: a lane needs 8 packed
+// registers per channel.  Here a packed register holds two CHANNELS of one
+// pixel's contribution, so each half of an accumulator is a distinct output:
+//  * a lane keeps CB/2 x 8 packed accumulators for CB channels (half the
+//    registers of the pixel-pair form), which leaves room for more warps;
+//  * the pixel's staged operands are duplicated into both halves
+//    ((re, re), (im, im), (-re, -re) per correlation, or a, a + b, b - a for
+//    the Gauss form) and read with 16-byte loads;
+//  * the phase of a channel pair is one packed FMA, x = (tau0, tau0) +
+//    (kappa_c, kappa_c+1) * (Q, Q), with tau0 and Q computed once per pixel and
+//    group in scalar FP32 from the FP64-derived per-timestep coefficients.
+// Work split: a visibility group is one timestep x CB channels; the four lanes
+// of a group each sum a quarter of the staged pixels; their partial sums are
+// combined with two levels of 64-bit warp shuffles and each lane writes CB/4
+// channels.
+#include "idg_device.cuh"
+#include "idg_internal.h"
+#include "idg_ptx.cuh"
+
+namespace idg {
+
+namespace {
+
+constexpr int kLanes = 4;             // lanes per visibility group
+constexpr int kGroupsPerWarp = 32 / kLanes;
+constexpr int kTimeTile = 64;
+constexpr int kMaxCB = 16;
+constexpr float kFastBound = 48.f;
+constexpr int kGaussCp = 4;           // FLAGS bit: three-multiplication MACs
+
+constexpr float kInv2Pi = 0.159154943091895335769f;
+constexpr float k2PiHi = 6.28125f;
+constexpr float k2PiLo = 1.9353071795864769253e-3f;
+
+struct Head {
+    int next, fast, qmax_bits, kmax_bits;
+};
+
+struct Layout {
+    size_t pix, geo, coef, kappa, total;
+};
+
+__host__ __device__ inline Layout layout(int S, int C, int batch) {
+    Layout L;
+    size_t off = 64;
+    L.pix = off;   off += (size_t)batch * 96;             // 12 packed operands per pixel
+    L.geo = off;   off += (size_t)S * S * 16;             // (hx, hy, n, 0) per pixel
+    L.coef = off;  off += (size_t)kTimeTile * 32;         // (a, b, g, qu) (qv, qw, -, -) per timestep
+    L.kappa = off; off += (size_t)(C + kMaxCB) * 4;       // kappa per channel, zero padded
+    L.total = (off + 15) & ~size_t(15);
+    return L;
+}
+
+// x - 2 pi rint(x / 2 pi) (Cody-Waite, two constants)
+__device__ __forceinline__ float reduce_2pi_s(float x) {
+    const float k = rintf(x * kInv2Pi);
+    return fmaf(k, -k2PiLo, fmaf(k, -k2PiHi, x));
+}
+__device__ __forceinline__ f2 reduce_2pi(f2 x) {
+    const f2 M = pack2(12582912.0f, 12582912.0f);
+    f2 k = fmul2(x, pack2(kInv2Pi, kInv2Pi));
+    k = fsub2(fadd2(k, M), M);
+    x = ffma2(k, pack2(-k2PiHi, -k2PiHi), x);
+    return ffma2(k, pack2(-k2PiLo, -k2PiLo), x);
+}
+
+__device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
+    float x0, x1, s0, c0, s1, c1;
+    unpack2(x, x0, x1);
+    __sincosf(x0, &s0, &c0);
+    __sincosf(x1, &s1, &c1);
+    c = pack2(c0, c1);
+    s = pack2(s0, s1);
+}
+
+// One pixel's contribution to the group's channel pairs.
+// Four-multiplication form, V += P (cos - i sin): re += pr c + pi s, im += pi c - pr s;
+// operands o[3k] = (pr, pr), o[3k+1] = (pi, pi), o[3k+2] = (-pr, -pr).
+// Gauss form: k1 = pr (cos - sin), -k2 = (pr + pi) sin, k3 = (pi - pr) cos,
+// Re = k1 + (-k2), Im = k1 + k3; operands a, a + b, b - a.
+template <int NPAIR, bool FAST, bool GAUSS, int NACC>
+__device__ __forceinline__ void pixel_macs(f2 (&acc)[NPAIR][NACC], const f2 (&kp)[NPAIR], f2 tau2, f2 Q2,
+                                           uint32_t ops_addr) {
+    f2 o[12];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) lds2(ops_addr + 16 * q, o[2 * q], o[2 * q + 1]);
+#pragma unroll
+    for (int j = 0; j < NPAIR; ++j) {
+        f2 x = ffma2(kp[j], Q2, tau2);
+        if (!FAST) x = reduce_2pi(x);
+        f2 C, Sn;
+        sincos_pair(x, C, Sn);
+        if (GAUSS) {
+            const f2 cms = fsub2(C, Sn);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                acc[j][3 * k] = ffma2(o[3 * k], cms, acc[j][3 * k]);
+                acc[j][3 * k + 1] = ffma2(o[3 * k + 1], Sn, acc[j][3 * k + 1]);
+                acc[j][3 * k + 2] = ffma2(o[3 * k + 2], C, acc[j][3 * k + 2]);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                acc[j][2 * k] = ffma2(o[3 * k + 1], Sn, ffma2(o[3 * k], C, acc[j][2 * k]));
+                acc[j][2 * k + 1] = ffma2(o[3 * k + 2], Sn, ffma2(o[3 * k + 1], C, acc[j][2 * k + 1]));
+            }
+        }
+    }
+}
+
+template <int NPAIR, bool FAST, bool GAUSS, int NACC, int UNR>
+__device__ __forceinline__ void group_pixels(f2 (&acc)[NPAIR][NACC], const f2 (&kp)[NPAIR], float A, float B, float Gc,
+                                             float qu, float qv, float qw, const float4 *geo, uint32_t pix_addr,
+                                             int pb, int part, int np) {
+#pragma unroll UNR
+    for (int i = part; i < np; i += kLanes) {
+        const float4 g = geo[pb + i];
+        const float tau0 = reduce_2pi_s(fmaf(A, g.x, fmaf(B, g.y, Gc * g.z)));
+        const float Q = fmaf(qu, g.x, fmaf(qv, g.y, qw * g.z));
+        pixel_macs<NPAIR, FAST, GAUSS, NACC>(acc, kp, pack2(tau0, tau0), pack2(Q, Q), pix_addr + 96u * (uint32_t)i);
+    }
+}
+
+// NT threads, BATCH pixels staged per pass, at least MINB CTAs per SM, CB
+// channels per group (8 or 16), FLAGS: kGaussCp; UNR: pixel-loop unrolling.
+template <int NT, int BATCH, int MINB, int CB, int FLAGS, int UNR>
+__global__ void __launch_bounds__(NT, MINB) degridder_cp_kernel(KernelArgs a) {
+    constexpr int kT = NT, kCB = CB, kNP = CB / 2;
+    constexpr bool kG = (FLAGS & kGaussCp) != 0;
+    constexpr int kAcc = kG ? 12 : 8;
+    static_assert(CB == 8 || CB == 16, "channel groups of 8 or 16");
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int S = a.S, S2 = S * S;
+    const Layout L = layout(S, a.C, BATCH);
+    Head *head = reinterpret_cast<Head *>(smem);
+    float4 *pix = reinterpret_cast<float4 *>(smem + L.pix);
+    float4 *geo = reinterpret_cast<float4 *>(smem + L.geo);
+    float4 *coef = reinterpret_cast<float4 *>(smem + L.coef);
+    float *kap = reinterpret_cast<float *>(smem + L.kappa);
+    const uint32_t pix_addr = smem_addr(pix);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gw = lane / kLanes, part = lane % kLanes;
+    const bool refcpu = (a.flags & IDG_FLAG_DEGRID_ATERM_REFCPU) != 0;
+    const bool taper = (a.flags & IDG_FLAG_NO_TAPER) == 0;
+
+    for (int q = tid; q < S2; q += kT) {
+        const float3 g = pixel_geometry(q, S, a.image_size);
+        geo[q] = make_float4(g.x, g.y, g.z, 0.f);
+    }
+    const double d2pi = (double)a.image_size / (double)S / kTwoPi;
+    const float hmax = 0.5f * (float)(S - 1);
+    const float nmax = pixel_geometry(0, S, a.image_size).z;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            head->next = atomicAdd(a.work_counter, 1);
+            head->kmax_bits = 0;
+            head->qmax_bits = 0;
+        }
+        __syncthreads();
+        const int idx = head->next;
+        if (idx >= a.nr_subgrids) break;
+        const int s = a.work_list ? a.work_list[idx] : idx;
+        const SubgridInfo si = load_subgrid(a, s);
+        if (!si.ok) {
+            if (tid == 0) flag_status(a.status, kStatusBadPlan);
+            continue;
+        }
+        const int nc = si.c1 - si.c0;
+        const int ncb = (nc + kCB - 1) / kCB;
+        const int cref = si.c0 + (nc > 0 ? (nc - 1) / 2 : 0);
+        const double kref = nc > 0 ? (double)a.wavenumbers[cref] : 0.0;
+        float kmax = 0.f;
+        for (int c = tid; c < ncb * kCB; c += kT) {
+            float kv = 0.f;
+            if (c < nc) kv = (float)((double)a.wavenumbers[si.c0 + c] - kref);
+            kap[c] = kv;
+            kmax = fmaxf(kmax, fabsf(kv));
+        }
+        if (kmax > 0.f) atomicMax(&head->kmax_bits, __float_as_int(kmax));
+        const size_t jones_stride = (size_t)S2 * 2;
+        const float4 *a1 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st1) * jones_stride;
+        const float4 *a2 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st2) * jones_stride;
+
+        for (int pb = 0; pb < S2; pb += BATCH) {
+            const int np = min(BATCH, S2 - pb);
+            __syncthreads(); // previous batch consumed
+            // ---- stage prepared pixels (A-terms and taper applied), operands duplicated
+            for (int i = tid; i < np; i += kT) {
+                const int q = pb + i;
+                const float sph = taper ? a.taper[q] : 1.f;
+                cf v[4];
+#pragma unroll
+                for (int pol = 0; pol < 4; ++pol) {
+                    const float2 x = a.subgrids[((size_t)s * 4 + pol) * S2 + q];
+                    v[pol] = {sph * x.x, sph * x.y};
+                }
+                cf j1[4], j2[4];
+                load_jones(a1 + 2 * q, j1);
+                load_jones(a2 + 2 * q, j2);
+                if (refcpu)
+                    aterm_gridder(v, j1, j2);
+                else
+                    aterm_adjoint(v, j1, j2);
+                float e[12];
+#pragma unroll
+                for (int pol = 0; pol < 4; ++pol) {
+                    if (kG) {
+                        e[3 * pol] = v[pol].re;
+                        e[3 * pol + 1] = v[pol].re + v[pol].im;
+                        e[3 * pol + 2] = v[pol].im - v[pol].re;
+                    } else {
+                        e[3 * pol] = v[pol].re;
+                        e[3 * pol + 1] = v[pol].im;
+                        e[3 * pol + 2] = -v[pol].re;
+                    }
+                }
+                float4 *d = pix + 6 * i;
+#pragma unroll
+                for (int r = 0; r < 6; ++r) d[r] = make_float4(e[2 * r], e[2 * r], e[2 * r + 1], e[2 * r + 1]);
+            }
+
+            for (int t0 = 0; t0 < si.T; t0 += kTimeTile) {
+                const int tt = min(kTimeTile, si.T - t0);
+                __syncthreads();
+                for (int t = tid; t < tt; t += kT) {
+                    const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
+                    const double u = p[0], v = p[1], w = p[2];
+                    double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
+                    double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
+                    ca -= 2.0 * rint(ca * 0.5);
+                    cbv -= 2.0 * rint(cbv * 0.5);
+                    const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
+                    const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
+                    coef[2 * t + 0] = make_float4((float)(kTwoPi * ca), (float)(kTwoPi * cbv), (float)cg, qu);
+                    coef[2 * t + 1] = make_float4(qv, qw, 0.f, 0.f);
+                    atomicMax(&head->qmax_bits, __float_as_int(fabsf(qu) * hmax + fabsf(qv) * hmax + fabsf(qw) * nmax));
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    head->fast = (3.1416f + __int_as_float(head->kmax_bits) * __int_as_float(head->qmax_bits)) <= kFastBound;
+                    head->qmax_bits = 0;
+                }
+                __syncthreads();
+                const bool fast = head->fast != 0;
+                const int ngroups = tt * ncb;
+                for (int gbase = warp * kGroupsPerWarp; gbase < ngroups; gbase += (kT / 32) * kGroupsPerWarp) {
+                    const int grp = gbase + gw;
+                    const bool active = grp < ngroups;
+                    const int gg = active ? grp : 0;
+                    const int t = gg / ncb, cfirst = (gg - t * ncb) * kCB;
+                    const float4 c0 = coef[2 * t], c1 = coef[2 * t + 1];
+                    f2 kp[kNP];
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j) kp[j] = pack2(kap[cfirst + 2 * j], kap[cfirst + 2 * j + 1]);
+                    f2 acc[kNP][kAcc];
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j)
+#pragma unroll
+                        for (int r = 0; r < kAcc; ++r) acc[j][r] = 0ull;
+                    if (fast)
+                        group_pixels<kNP, true, kG, kAcc, UNR>(acc, kp, c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, geo,
+                                                               pix_addr, pb, part, np);
+                    else
+                        group_pixels<kNP, false, kG, kAcc, UNR>(acc, kp, c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, geo,
+                                                                pix_addr, pb, part, np);
+                    // combine the four lanes: both halves of a register are distinct channels
+                    f2 out[kNP][8];
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j)
+#pragma unroll
+                        for (int r = 0; r < 8; ++r) {
+                            f2 v = kG ? fadd2(acc[j][3 * (r / 2)], acc[j][3 * (r / 2) + 1 + (r & 1)]) : acc[j][r];
+                            v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 1));
+                            v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 2));
+                            out[j][r] = v;
+                        }
+                    if (active) {
+                        float4 *row = a.vis + ((int64_t)si.row0 + t0 + t) * a.C * 2;
+#pragma unroll
+                        for (int j = 0; j < kNP; ++j) {
+                            if (j % kLanes != part) continue;
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                if (cfirst + 2 * j + h >= nc) continue;
+                                const int c = si.c0 + cfirst + 2 * j + h;
+                                float w[8];
+#pragma unroll
+                                for (int r = 0; r < 8; ++r) {
+                                    float lo, hi;
+                                    unpack2(out[j][r], lo, hi);
+                                    w[r] = h ? hi : lo;
+                                }
+                                float4 va = make_float4(w[0], w[1], w[2], w[3]);
+                                float4 vb = make_float4(w[4], w[5], w[6], w[7]);
+                                if (pb > 0) {
+                                    const float4 oa = row[2 * c], ob = row[2 * c + 1];
+                                    va = make_float4(va.x + oa.x, va.y + oa.y, va.z + oa.z, va.w + oa.w);
+                                    vb = make_float4(vb.x + ob.x, vb.y + ob.y, vb.z + ob.z, vb.w + ob.w);
+                                }
+                                row[2 * c] = va;
+                                row[2 * c + 1] = vb;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int NT, int BATCH, int MINB, int CB, int FLAGS, int UNR>
+cudaError_t launch_cp(const KernelArgs &a, cudaStream_t stream) {
+    auto kern = degridder_cp_kernel<NT, BATCH, MINB, CB, FLAGS, UNR>;
+    const size_t smem = layout(a.S, a.C, BATCH).total;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (a.max_ctas > 0 && blocks > a.max_ctas) blocks = a.max_ctas;
+    if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
+    kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+int degridder_cp_shapes() { return 13; }
+
+// Channel-pair shapes (index within this family):
+//   0: 128 threads, 8-channel groups, 256-pixel batches, 4 CTAs/SM (16 warps)
+//   1: 128 threads, 8-channel groups, 3 CTAs/SM, pixel loop unrolled by two
+//   2: 128 threads, 16-channel groups, 2 CTAs/SM
+//   3: 128 threads, 8-channel groups, Gauss MACs, 3 CTAs/SM
+//   4: 256 threads, 8-channel groups, 2 CTAs/SM (16 warps)
+//   5: 128 threads, 16-channel groups, Gauss MACs, 2 CTAs/SM
+//   6: 128 threads, 8-channel groups, Gauss MACs, 2 CTAs/SM (registers uncapped)
+//   7: shape 6 with the pixel loop unrolled by two
+//   8: 128 threads, 8-channel groups, 2 CTAs/SM, pixel loop unrolled by two
+//   9: shape 6 with the pixel loop unrolled by four
+//  10: shape 7 with 256-pixel batches
+//  11: shape 8 with the pixel loop unrolled by four
+//  12: shape 6 with the pixel loop unrolled by eight
+cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int shape) {
+    switch (shape) {
+    case 1: return launch_cp<128, 512, 3, 8, 0, 2>(a, stream);
+    case 2: return launch_cp<128, 512, 2, 16, 0, 1>(a, stream);
+    case 3: return launch_cp<128, 512, 3, 8, kGaussCp, 1>(a, stream);
+    case 4: return launch_cp<256, 512, 2, 8, 0, 1>(a, stream);
+    case 5: return launch_cp<128, 512, 2, 16, kGaussCp, 1>(a, stream);
+    case 6: return launch_cp<128, 512, 2, 8, kGaussCp, 1>(a, stream);
+    case 7: return launch_cp<128, 512, 2, 8, kGaussCp, 2>(a, stream);
+    case 8: return launch_cp<128, 512, 2, 8, 0, 2>(a, stream);
+    case 9: return launch_cp<128, 512, 2, 8, kGaussCp, 4>(a, stream);
+    case 10: return launch_cp<128, 256, 2, 8, kGaussCp, 2>(a, stream);
+    case 11: return launch_cp<128, 512, 2, 8, 0, 4>(a, stream);
+    case 12: return launch_cp<128, 512, 2, 8, kGaussCp, 8>(a, stream);
+    default: return launch_cp<128, 256, 4, 8, 0, 1>(a, stream);
+    }
+}
+
+} // namespace idg

@@ -141,6 +141,23 @@ __device__ __forceinline__ void pair_macs(f2 (&acc)[kCB][12], const f2 (&kc)[kCB
     }
 }
 
+// One lane's share of a visibility group: pixel pairs part, part + 4, ... of
+// the staged batch (the 4 lanes of a group split the batch).  The FAST/slow
+// phase path is chosen once per group, outside the pixel loop.
+template <int kCB, bool FAST, int FLAGS, int NACC>
+__device__ __forceinline__ void group_pixels(f2 (&acc)[kCB][NACC], const f2 (&kc)[kCB], f2 A2, f2 B2, f2 G2, f2 QU,
+                                             f2 QV, f2 QW, const f2 *geo, const float4 *pix, int pb, int part, int np) {
+    constexpr bool FTZ = (FLAGS & kFtz) != 0;
+#pragma unroll((FLAGS & kUnroll2) ? 2 : 1)
+    for (int i = part; i < np; i += kLanesPerGroup) {
+        const int p = pb + i;
+        const f2 hx = geo[3 * p], hy = geo[3 * p + 1], nn = geo[3 * p + 2];
+        const f2 tau0 = reduce_2pi(ffma2(A2, hx, ffma2(B2, hy, fmul2(G2, nn))));
+        const f2 Q = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
+        pair_macs<kCB, FAST, FTZ>(acc, kc, tau0, Q, pix + 6 * i);
+    }
+}
+
 // Kernel shape: NT threads per CTA, BATCH pixel pairs staged per pass, at least
 // MINB CTAs per SM (register cap), CB channels per visibility group (the
 // per-(pixel pair, timestep) phase terms are computed once per group, so a
@@ -302,17 +319,10 @@ __global__ void __launch_bounds__(NT, MINB) degridder_fast_kernel(KernelArgs a) 
 #pragma unroll
                         for (int r = 0; r < kAcc; ++r) acc[j][r] = 0ull;
 
-#pragma unroll((FLAGS & kUnroll2) ? 2 : 1)
-                    for (int i = part; i < np; i += kLanesPerGroup) {
-                        const int p = pb + i;
-                        const f2 hx = geo[3 * p], hy = geo[3 * p + 1], nn = geo[3 * p + 2];
-                        const f2 tau0 = reduce_2pi(ffma2(A2, hx, ffma2(B2, hy, fmul2(G2, nn))));
-                        const f2 Q = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
-                        if (fast)
-                            pair_macs<kCB, true, FTZ>(acc, kc, tau0, Q, pix + 6 * i);
-                        else
-                            pair_macs<kCB, false, FTZ>(acc, kc, tau0, Q, pix + 6 * i);
-                    }
+                    if (fast)
+                        group_pixels<kCB, true, FLAGS>(acc, kc, A2, B2, G2, QU, QV, QW, geo, pix, pb, part, np);
+                    else
+                        group_pixels<kCB, false, FLAGS>(acc, kc, A2, B2, G2, QU, QV, QW, geo, pix, pb, part, np);
                     // fold the pair halves, then combine the four lanes of the group
                     float vsum[kCB][8];
 #pragma unroll
@@ -374,9 +384,11 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 } // namespace
 
 // Launch shapes of the batched degridder (index = shape id).
-int degridder_fast_shapes() { return 15; }
+// Shapes 0-14 are the pixel-pair kernel above; 15 and up the channel-pair kernel.
+int degridder_fast_shapes() { return 15 + degridder_cp_shapes(); }
 
 cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
+    if (shape >= 15) return launch_degridder_cp(a, stream, shape - 15);
     switch (shape) {
     case 1: return launch_shape<128, 512, 4>(a, stream); // 16 warps/SM, register cap 128
     case 2: return launch_shape<256, 512, 2>(a, stream); // 16 warps/SM in 256-thread CTAs

@@ -159,6 +159,7 @@ constexpr int kPipe = 1;     // software-pipelined channel loop
 constexpr int kFtz = 2;      // SFU sine/cosine flushing subnormal arguments
 constexpr int kGauss = 4;    // three-multiplication MACs (12 accumulators per pair)
 constexpr int kUnroll2 = 8;  // channel loop unrolled by two
+constexpr int kUnroll4 = 16; // channel loop unrolled by four
 
 // One staged tile: tt timesteps x ncc channels.
 // PIPE & kPipe: the channel loop is software pipelined -- the sincos of channel
@@ -213,7 +214,7 @@ template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
     constexpr int kT = NT, kPairs = PAIRS, kPassPairs = NT * PAIRS, kTileVis = TV, kMaxChunk = TV;
     constexpr bool kG = (PIPE & kGauss) != 0;
-    constexpr int kAcc = kG ? 12 : 8, kUnr = (PIPE & kUnroll2) ? 2 : 1;
+    constexpr int kAcc = kG ? 12 : 8, kUnr = (PIPE & kUnroll4) ? 4 : (PIPE & kUnroll2) ? 2 : 1;
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = a.S, S2 = S * S, npairs = S2 / 2;
     const Layout L = layout(S, a.C, TV);
@@ -441,6 +442,8 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 //  10: 128 x 4, 3 CTAs/SM, Gauss MACs
 //  11: 96 x 3 (288 pairs per pass: whole passes for S = 24 and 48), Gauss, pipelined, unrolled by two
 //  12: 128 x 3 (384 pairs per pass: whole passes for S = 48), Gauss, pipelined, unrolled by two
+//  13: shape 8 with the channel loop unrolled by four
+//  14: shape 7 with the channel loop unrolled by four
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -462,7 +465,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return 13; }
+int gridder_fast_shapes() { return 15; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -478,6 +481,8 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 10: return launch_shape<128, 4, 256, 3, kGauss>(a, stream);
     case 11: return launch_shape<96, 3, 256, 3, kGauss | kPipe | kUnroll2>(a, stream);
     case 12: return launch_shape<128, 3, 256, 2, kGauss | kPipe | kUnroll2>(a, stream);
+    case 13: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll4>(a, stream);
+    case 14: return launch_shape<128, 4, 256, 2, kGauss | kUnroll4>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }

@@ -20,6 +20,9 @@ int batched_gridder_shape(int S);
 void set_batched_gridder_shape(int S, int shape);
 cudaError_t launch_degridder_fast(const KernelArgs &a, cudaStream_t stream, int shape);
 int degridder_fast_shapes();
+// Channel-pair-packed batched degridder (idg_degridder_cp.cu), shapes 0..degridder_cp_shapes()-1.
+cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int shape);
+int degridder_cp_shapes();
 int batched_degridder_shape(int S);
 void set_batched_degridder_shape(int S, int shape);
 
