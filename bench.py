@@ -47,9 +47,9 @@ METRIC = "Mvis/s grid+degrid vs plain GPU form at ≤1e-5 rel err; p50/p99 job l
 FLOP_PER_PIXVIS = 34.0  # 16 FMA of the four complex MACs + 1 FMA of the phase
 # DRAM bytes (read + write) per subgrid of one batched kernel launch, S = 32, 16
 # channels x 128 timesteps: ncu capture of one launch on the first 8192
-# subgrids of the config-2 plan (gridder 687.5 MB read + 244.6 MB written;
-# degridder 418.7 MB read + 490.3 MB written), divided by 8192.
-DRAM_BYTES_PER_SUBGRID = {"gridder": 113786.0, "degridder": 110969.0}
+# subgrids of the config-2 plan with the tuned shapes (gridder 686.6 MB read +
+# 244.7 MB written; degridder 419.7 MB read + 490.9 MB written), divided by 8192.
+DRAM_BYTES_PER_SUBGRID = {"gridder": 113682.0, "degridder": 111153.0}
 
 
 def parse():
