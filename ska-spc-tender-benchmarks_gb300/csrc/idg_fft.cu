@@ -12,9 +12,10 @@
 // which is where the e^{i pi j/S} factors come from.
 //
 // Kernel: a CTA transforms PLANES (subgrid, polarisation) planes.  Planes are
-// loaded with coalesced 8-byte accesses into padded shared memory, one thread
-// per row runs a register-resident radix-2 (x radix-3 for S = 24, 48) FFT,
-// then one thread per column does the same, and the planes are stored back.
+// loaded with coalesced 16-byte accesses, eight in flight per thread, into
+// padded shared memory; one thread per row runs a register-resident radix-2
+// (x radix-3 for S = 24, 48) FFT, then one thread per column does the same,
+// and the planes are stored back with 16-byte stores.
 #include "idg_device.cuh"
 #include "idg_internal.h"
 
@@ -23,41 +24,54 @@ namespace idg {
 namespace {
 
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
+// Bit reversal of i in `bits` <= 6 bits, as one straight-line expression so
+// that it folds to a constant inside fully unrolled loops (a loop here left the
+// register arrays indexed at run time, i.e. in local memory).
 __host__ __device__ constexpr int bitrev(int i, int bits) {
-    int r = 0;
-    for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
-    return r;
+    return ((((i >> 0) & 1) << 5) | (((i >> 1) & 1) << 4) | (((i >> 2) & 1) << 3) | (((i >> 3) & 1) << 2) |
+            (((i >> 4) & 1) << 1) | ((i >> 5) & 1)) >> (6 - bits);
+}
+
+// Compile-time bit-reversal permutation of x[0..M) (template recursion: every
+// index is a constant, so x stays in registers).
+template <int M, int I = 0>
+__device__ __forceinline__ void bitrev_permute(cf *x) {
+    if constexpr (I < M) {
+        constexpr int J = bitrev(I, ilog2(M));
+        if constexpr (J > I) {
+            const cf t = x[I];
+            x[I] = x[J];
+            x[J] = t;
+        }
+        bitrev_permute<M, I + 1>(x);
+    }
+}
+
+// Radix-2 butterflies of stage LEN (and, recursively, the later stages).
+template <int M, int N, int SIGN, int LEN>
+__device__ __forceinline__ void fft_stages(cf *x, const float2 *tw) {
+#pragma unroll
+    for (int i0 = 0; i0 < M; i0 += LEN) {
+#pragma unroll
+        for (int j = 0; j < LEN / 2; ++j) {
+            const float2 w2 = tw[j * (N / LEN)];
+            const cf w = {w2.x, SIGN > 0 ? w2.y : -w2.y};
+            const cf u = x[i0 + j];
+            const cf v = (j == 0) ? x[i0 + j + LEN / 2] : cmul(x[i0 + j + LEN / 2], w);
+            x[i0 + j] = cadd(u, v);
+            x[i0 + j + LEN / 2] = {u.re - v.re, u.im - v.im};
+        }
+    }
+    if constexpr (LEN < M) fft_stages<M, N, SIGN, 2 * LEN>(x, tw);
 }
 
 // In-register radix-2 DIT FFT of M = 2^k points x[0..M) whose twiddles come
 // from tw[m] = e^{+2 pi i m / N} (M divides N).  SIGN = +1 or -1.
 template <int M, int N, int SIGN>
 __device__ __forceinline__ void fft_pow2(cf *x, const float2 *tw) {
-    constexpr int bits = ilog2(M);
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        const int j = bitrev(i, bits);
-        if (j > i) {
-            const cf t = x[i];
-            x[i] = x[j];
-            x[j] = t;
-        }
-    }
-#pragma unroll
-    for (int len = 2; len <= M; len <<= 1) {
-#pragma unroll
-        for (int i0 = 0; i0 < M; i0 += len) {
-#pragma unroll
-            for (int j = 0; j < len / 2; ++j) {
-                const float2 w2 = tw[j * (N / len)];
-                const cf w = {w2.x, SIGN > 0 ? w2.y : -w2.y};
-                const cf u = x[i0 + j];
-                const cf v = (j == 0) ? x[i0 + j + len / 2] : cmul(x[i0 + j + len / 2], w);
-                x[i0 + j] = cadd(u, v);
-                x[i0 + j + len / 2] = {u.re - v.re, u.im - v.im};
-            }
-        }
-    }
+    static_assert(M <= 64, "bitrev handles up to 6 bits");
+    bitrev_permute<M>(x);
+    if constexpr (M > 1) fft_stages<M, N, SIGN, 2>(x, tw);
 }
 
 // Length-N FFT with N = 2^k or 3 * 2^k, in registers.
@@ -110,8 +124,11 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
     __shared__ float2 tw[S];      // e^{+2 pi i m / S}
     __shared__ float2 post[S];    // c_j = (-1)^j e^{+i pi (j - S/2)/S}
     __shared__ float2 buf[Sh::planes][S][Sh::pitch];
+    __shared__ float tp[S * S];   // taper (ones when none is given)
+    constexpr int kBatch = 8;     // 16-byte loads in flight per thread
 
     const int tid = threadIdx.x;
+    for (int q = tid; q < S * S; q += Sh::threads) tp[q] = taper ? taper[q] : 1.f;
     if (tid < S) {
         double s, c;
         sincospi(2.0 * tid / S, &s, &c);
@@ -124,20 +141,38 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
     const int nplanes = (int)min((int64_t)Sh::planes, nr_planes - plane0);
     __syncthreads();
 
-    // load + pre-multiply
-    for (int e = tid; e < nplanes * S * S; e += Sh::threads) {
-        const int pl = e / (S * S), q = e - pl * S * S, y = q / S, x = q - y * S;
-        float2 v = data[(plane0 + pl) * S * S + q];
-        if (DIR > 0) {
-            const float f = (((x + y) & 1) ? -1.f : 1.f) * (taper ? taper[q] : 1.f);
-            v = make_float2(v.x * f, v.y * f);
-        } else {
-            const float2 cy = post[y], cx = post[x];
-            const cf w = cconj(cmul({cy.x, cy.y}, {cx.x, cx.y}));
-            const cf r = cmul({v.x, v.y}, w);
-            v = make_float2(r.re, r.im);
+    // load + pre-multiply: two complex values per 16-byte load, a batch of
+    // independent loads in flight per thread before any of them is used
+    const int total2 = nplanes * S * S / 2;  // float4 elements of this CTA's planes
+    const float4 *src = reinterpret_cast<const float4 *>(data + plane0 * S * S);
+    for (int base = 0; base < total2; base += kBatch * Sh::threads) {
+        float4 v[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) {
+            const int e2 = base + tid + k * Sh::threads;
+            v[k] = e2 < total2 ? src[e2] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        buf[pl][y][x] = v;
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) {
+            const int e2 = base + tid + k * Sh::threads;
+            if (e2 >= total2) continue;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int e = 2 * e2 + h;
+                const int pl = e / (S * S), q = e - pl * S * S, y = q / S, x = q - y * S;
+                float2 w = h ? make_float2(v[k].z, v[k].w) : make_float2(v[k].x, v[k].y);
+                if (DIR > 0) {
+                    const float f = (((x + y) & 1) ? -1.f : 1.f) * tp[q];
+                    w = make_float2(w.x * f, w.y * f);
+                } else {
+                    const float2 cy = post[y], cx = post[x];
+                    const cf c = cconj(cmul({cy.x, cy.y}, {cx.x, cx.y}));
+                    const cf r = cmul({w.x, w.y}, c);
+                    w = make_float2(r.re, r.im);
+                }
+                buf[pl][y][x] = w;
+            }
+        }
     }
     __syncthreads();
 
@@ -160,19 +195,26 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
     }
     __syncthreads();
 
-    // post-multiply + store
-    for (int e = tid; e < nplanes * S * S; e += Sh::threads) {
-        const int pl2 = e / (S * S), q = e - pl2 * S * S, y = q / S, xx = q - y * S;
-        float2 v = buf[pl2][y][xx];
-        if (DIR > 0) {
-            const float2 cy = post[y], cx = post[xx];
-            const cf r2 = cmul(cmul({v.x, v.y}, {cy.x, cy.y}), {cx.x, cx.y});
-            v = make_float2(r2.re, r2.im);
-        } else {
-            const float f = (((xx + y) & 1) ? -1.f : 1.f) * (taper ? taper[q] : 1.f);
-            v = make_float2(v.x * f, v.y * f);
+    // post-multiply + store, two complex values per 16-byte store
+    float4 *dst = reinterpret_cast<float4 *>(data + plane0 * S * S);
+    for (int e2 = tid; e2 < total2; e2 += Sh::threads) {
+        float2 o[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int e = 2 * e2 + h;
+            const int pl2 = e / (S * S), q = e - pl2 * S * S, y = q / S, xx = q - y * S;
+            float2 v = buf[pl2][y][xx];
+            if (DIR > 0) {
+                const float2 cy = post[y], cx = post[xx];
+                const cf r2 = cmul(cmul({v.x, v.y}, {cy.x, cy.y}), {cx.x, cx.y});
+                v = make_float2(r2.re, r2.im);
+            } else {
+                const float f = (((xx + y) & 1) ? -1.f : 1.f) * tp[q];
+                v = make_float2(v.x * f, v.y * f);
+            }
+            o[h] = v;
         }
-        data[(plane0 + pl2) * S * S + q] = v;
+        dst[e2] = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
     }
 }
 
