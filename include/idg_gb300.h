@@ -167,6 +167,19 @@ IDG_API int idg_adder(const idg_params *params, int64_t nr_subgrids, const idg_m
 IDG_API int idg_splitter(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
                          const void *grid, void *subgrids, void *stream);
 
+/* In-place 2-D FFT of every plane of grid[W][4][G][G] (G a power of two,
+ * 64 <= G <= 8192), the imaging step around the path:
+ *   direction -1 (uv -> image):
+ *     out[y][x] = c[y] c[x] sum_{v,u} grid[v][u] exp(-2 pi i((u-G/2)(x-G/2) + (v-G/2)(y-G/2))/G)
+ *   direction +1 (image -> uv): the adjoint (c applied before the transform).
+ * `correction` is a DEVICE array of G floats (the separable grid correction,
+ * e.g. the reciprocal of the taper's transform) or NULL (c = 1).  No
+ * normalisation.  The first call for a (device, G) allocates and uploads a
+ * twiddle table (so that call is not stream-capturable).  The reference
+ * benchmarks this transform separately (fft/, heFFTe). */
+IDG_API int idg_grid_fft(const idg_params *params, void *grid, int direction, const float *correction,
+                         void *stream);
+
 /* ------------------------------------------------------------------ */
 /* The gridding / degridding steps on device-resident data             */
 /* ------------------------------------------------------------------ */

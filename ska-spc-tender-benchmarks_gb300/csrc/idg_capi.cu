@@ -259,6 +259,20 @@ IDG_API int idg_splitter(const idg_params *params, int64_t nr_subgrids, const id
     return IDG_OK;
 }
 
+IDG_API int idg_grid_fft(const idg_params *params, void *grid, int direction, const float *correction,
+                         void *stream) {
+    if (!params) return fail(IDG_ERR_INVALID_ARGUMENT, "params is NULL");
+    const int G = params->grid_size, W = params->nr_w_planes > 0 ? params->nr_w_planes : 1;
+    if (!grid_fft_size_supported(G))
+        return fail(IDG_ERR_UNSUPPORTED, "grid size %d: the grid FFT takes powers of two from 64 to 8192", G);
+    if (direction != 1 && direction != -1) return fail(IDG_ERR_INVALID_ARGUMENT, "direction must be +1 or -1");
+    if (!grid || !aligned16(grid)) return fail(IDG_ERR_INVALID_ARGUMENT, "grid must be a 16-byte aligned device pointer");
+    cudaError_t e = launch_grid_fft(reinterpret_cast<float2 *>(grid), G, 4 * W, direction, correction,
+                                    reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "grid FFT");
+    return IDG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Drop-in launchers
 // ---------------------------------------------------------------------------

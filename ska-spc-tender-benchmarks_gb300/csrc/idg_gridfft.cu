@@ -1,0 +1,215 @@
+// idg_gridfft.cu -- 2-D FFT of the uv-grid (the imaging step after the adder).
+//
+// For every plane (w-plane, polarisation) of grid[W][4][G][G], G = 2^k:
+//   direction -1 (uv -> image):
+//     out[y][x] = c[y] c[x] sum_{v,u} grid[v][u] exp(-2 pi i ((u-G/2)(x-G/2) + (v-G/2)(y-G/2)) / G)
+//   direction +1 (image -> uv): the adjoint,
+//     out[v][u] = sum_{y,x} c[y] c[x] grid[y][x] exp(+2 pi i ((u-G/2)(x-G/2) + (v-G/2)(y-G/2)) / G)
+// with c the optional separable grid correction (length G; 1 when NULL).  The
+// centre cell G/2 is the origin of both domains.  For G divisible by 4 the
+// shifts factorise into (-1)^(u+v) before and (-1)^(x+y) after an unshifted
+// DFT, so each 1-D pass is: multiply by (-1)^index (and c), unshifted FFT,
+// multiply by (-1)^index (and c).
+//
+// Passes per plane: row FFTs, tiled transpose, row FFTs, tiled transpose.  A
+// row FFT runs in one CTA: the row is staged in shared memory and transformed
+// by radix-4 Stockham stages (plus one radix-2 stage when log2 G is odd),
+// ping-ponging between two shared buffers; twiddles come from a table of
+// e^{-2 pi i m / G} computed in FP64 on the host.  All passes are HBM-bound:
+// 16 bytes per complex cell per pass (read + write).
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "idg_device.cuh"
+#include "idg_host.h"
+#include "idg_internal.h"
+
+namespace idg {
+
+namespace {
+
+constexpr int kRowThreads = 256;
+constexpr int kTile = 32;
+
+__device__ __forceinline__ float2 cm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+// One FFT over each row (length G, row stride G) of the CTA's row.  DIR = -1
+// uses e^{-2 pi i ...}, DIR = +1 its conjugate.  Element i of the row is
+// multiplied by (-1)^i before and after the transform (the centre shifts of
+// this dimension), and by corr[i] (when given) after it for DIR = -1 or before
+// it for DIR = +1.
+template <int DIR>
+__global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data, int G, int logG, const float2 *tw,
+                                                                   const float *corr) {
+    extern __shared__ float2 sm[];
+    float2 *A = sm, *B = sm + G;
+    const int row = blockIdx.x;
+    float2 *p = data + (int64_t)row * G;
+    // load (16-byte accesses), pre-multiply for the image -> uv direction
+    for (int i2 = threadIdx.x; i2 < G / 2; i2 += kRowThreads) {
+        const float4 v = reinterpret_cast<const float4 *>(p)[i2];
+        float2 a = make_float2(v.x, v.y), b = make_float2(v.z, v.w);
+        float fa = 1.f, fb = -1.f; // (-1)^i for i = 2 i2, 2 i2 + 1
+        if (DIR > 0 && corr) {
+            fa *= corr[2 * i2];
+            fb *= corr[2 * i2 + 1];
+        }
+        A[2 * i2] = make_float2(a.x * fa, a.y * fa);
+        A[2 * i2 + 1] = make_float2(b.x * fb, b.y * fb);
+    }
+    __syncthreads();
+    // Stockham stages: after a stage of radix R over sub-length L (L = product of
+    // the radices done so far), element (k, j) of the output holds the DFT of
+    // length L*R.  Indexing: n = G / (L*R) groups.
+    int L = 1;
+    float2 *src = A, *dst = B;
+    const int stages4 = logG / 2, has2 = logG & 1;
+    for (int st = 0; st < stages4 + has2; ++st) {
+        const int R = (st < stages4) ? 4 : 2;
+        const int LR = L * R, n = G / LR;
+        // butterflies: G / R of them; butterfly b = (q, k): q in [0, n), k in [0, L)
+        for (int b = threadIdx.x; b < G / R; b += kRowThreads) {
+            const int k = b % L, q = b / L;
+            // Stockham: inputs at stride G / R, outputs at q * L * R + k + r * L
+            float2 x[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (r < R) x[r] = src[b + r * (G / R)];
+            // twiddle for element r: w^(r*k) with w = e^{-2 pi i / LR}
+            if (k > 0) {
+#pragma unroll
+                for (int r = 1; r < 4; ++r)
+                    if (r < R) {
+                        const int m = (r * k) * n; // e^{-2 pi i r k / LR} = tw[r k n]
+                        const float2 w = DIR < 0 ? tw[m] : conjf2(tw[m]);
+                        x[r] = cm(x[r], w);
+                    }
+            }
+            float2 y[4];
+            if (R == 2) {
+                y[0] = make_float2(x[0].x + x[1].x, x[0].y + x[1].y);
+                y[1] = make_float2(x[0].x - x[1].x, x[0].y - x[1].y);
+            } else {
+                // radix-4 DFT with e^{DIR 2 pi i / 4} = DIR * i
+                const float2 s02 = make_float2(x[0].x + x[2].x, x[0].y + x[2].y);
+                const float2 d02 = make_float2(x[0].x - x[2].x, x[0].y - x[2].y);
+                const float2 s13 = make_float2(x[1].x + x[3].x, x[1].y + x[3].y);
+                const float2 d13 = make_float2(x[1].x - x[3].x, x[1].y - x[3].y);
+                // DIR < 0: y1 = d02 - i d13, y3 = d02 + i d13 (signs flipped for DIR > 0)
+                const float sgn = DIR < 0 ? 1.f : -1.f;
+                y[0] = make_float2(s02.x + s13.x, s02.y + s13.y);
+                y[2] = make_float2(s02.x - s13.x, s02.y - s13.y);
+                y[1] = make_float2(d02.x + sgn * d13.y, d02.y - sgn * d13.x);
+                y[3] = make_float2(d02.x - sgn * d13.y, d02.y + sgn * d13.x);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (r < R) dst[q * LR + k + r * L] = y[r];
+        }
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+        L = LR;
+    }
+    // post-multiply for the uv -> image direction, store
+    for (int i2 = threadIdx.x; i2 < G / 2; i2 += kRowThreads) {
+        float2 a = src[2 * i2], b = src[2 * i2 + 1];
+        float fa = 1.f, fb = -1.f;
+        if (DIR < 0 && corr) {
+            fa *= corr[2 * i2];
+            fb *= corr[2 * i2 + 1];
+        }
+        reinterpret_cast<float4 *>(p)[i2] = make_float4(a.x * fa, a.y * fa, b.x * fb, b.y * fb);
+    }
+}
+
+// In-place transpose of planes of G x G: CTA (bx, by) with bx >= by swaps tile
+// (by, bx) with tile (bx, by) (the diagonal tiles transpose in place).
+__global__ void __launch_bounds__(kTile * 8) grid_transpose_kernel(float2 *data, int G) {
+    __shared__ float2 ta[kTile][kTile + 1], tb[kTile][kTile + 1];
+    const int bx = blockIdx.x, by = blockIdx.y;
+    if (bx < by) return;
+    float2 *plane = data + (int64_t)blockIdx.z * G * G;
+    const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile; // 32 x 8
+    for (int j = ty; j < kTile; j += 8) {
+        ta[j][tx] = plane[(int64_t)(by * kTile + j) * G + bx * kTile + tx];
+        if (bx != by) tb[j][tx] = plane[(int64_t)(bx * kTile + j) * G + by * kTile + tx];
+    }
+    __syncthreads();
+    for (int j = ty; j < kTile; j += 8) {
+        plane[(int64_t)(bx * kTile + j) * G + by * kTile + tx] = ta[tx][j];
+        if (bx != by) plane[(int64_t)(by * kTile + j) * G + bx * kTile + tx] = tb[tx][j];
+    }
+}
+
+std::mutex g_tw_mutex;
+std::map<std::pair<int, int>, float2 *> g_tw; // (device, G) -> e^{-2 pi i m / G}, m < G
+
+cudaError_t twiddles(int G, const float2 **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(g_tw_mutex);
+    auto it = g_tw.find({dev, G});
+    if (it != g_tw.end()) {
+        *out = it->second;
+        return cudaSuccess;
+    }
+    std::vector<float2> h(G);
+    for (int m = 0; m < G; ++m) {
+        const double a = -2.0 * M_PI * (double)m / (double)G;
+        h[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    float2 *d = nullptr;
+    e = cudaMalloc(&d, sizeof(float2) * G);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(d, h.data(), sizeof(float2) * G, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return e;
+    }
+    g_tw[{dev, G}] = d;
+    *out = d;
+    return cudaSuccess;
+}
+
+} // namespace
+
+bool grid_fft_size_supported(int G) { return G >= 64 && G <= 8192 && (G & (G - 1)) == 0; }
+
+cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, const float *corr, cudaStream_t st) {
+    if (!grid_fft_size_supported(G)) return cudaErrorInvalidValue;
+    const float2 *tw = nullptr;
+    cudaError_t e = twiddles(G, &tw);
+    if (e != cudaSuccess) return e;
+    int logG = 0;
+    while ((1 << logG) < G) ++logG;
+    const size_t smem = 2 * sizeof(float2) * (size_t)G;
+    const int64_t rows = (int64_t)planes * G;
+    auto rowpass = [&]() -> cudaError_t {
+        if (direction < 0) {
+            cudaError_t e2 = cudaFuncSetAttribute(grid_row_fft_kernel<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e2 != cudaSuccess) return e2;
+            grid_row_fft_kernel<-1><<<(unsigned)rows, kRowThreads, smem, st>>>(grid, G, logG, tw, corr);
+        } else {
+            cudaError_t e2 = cudaFuncSetAttribute(grid_row_fft_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e2 != cudaSuccess) return e2;
+            grid_row_fft_kernel<1><<<(unsigned)rows, kRowThreads, smem, st>>>(grid, G, logG, tw, corr);
+        }
+        return cudaGetLastError();
+    };
+    const dim3 tgrid(G / kTile, G / kTile, planes);
+    // rows (x), transpose, rows (y), transpose back
+    if ((e = rowpass()) != cudaSuccess) return e;
+    grid_transpose_kernel<<<tgrid, kTile * 8, 0, st>>>(grid, G);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = rowpass()) != cudaSuccess) return e;
+    grid_transpose_kernel<<<tgrid, kTile * 8, 0, st>>>(grid, G);
+    return cudaGetLastError();
+}
+
+} // namespace idg

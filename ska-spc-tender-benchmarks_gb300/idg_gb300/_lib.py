@@ -174,6 +174,7 @@ _SIGNATURES = {
     "idg_subgrid_fft": [ctypes.POINTER(IdgParams), _I64, _I32, _P, _P, _P],
     "idg_adder": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
     "idg_splitter": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
+    "idg_grid_fft": [ctypes.POINTER(IdgParams), _P, _I32, _P, _P],
     "idg_grid_visibilities": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P],
     "idg_degrid_visibilities": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P],
     "idg_imaging_cycle": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64,

@@ -155,6 +155,18 @@ def splitter(spec: GridSpec, metadata, grid, subgrids, stream=None):
     return subgrids
 
 
+def grid_fft(spec: GridSpec, grid, direction: int, correction=None, stream=None):
+    """In-place 2-D FFT of every plane of grid[W,4,G,G] (idg_grid_fft): direction -1
+    uv -> image with the grid correction applied after, +1 image -> uv with it before."""
+    G, W = spec.grid_size, spec.nr_w_planes
+    _req(grid, "grid", torch.complex64, (W, 4, G, G))
+    if correction is not None:
+        _req(correction, "correction", torch.float32, (G,))
+    p = spec.to_c()
+    _lib.call("idg_grid_fft", ctypes.byref(p), ptr(grid), int(direction), ptr(correction), _stream_handle(stream))
+    return grid
+
+
 def grid_visibilities(spec: GridSpec, metadata, uvw, wavenumbers, vis, taper, aterms, subgrids, grid,
                       variant=VARIANT_BATCHED, ext=None, stream=None):
     """Gridding step: gridder -> subgrid FFT (+1, taper) -> adder; accumulates into grid[W,4,G,G]."""
