@@ -23,6 +23,8 @@ Printed (rank 0, one JSON line):
   serving p50 / p99 job latency and Mvis/s of a Poisson stream of gridding and
           degridding jobs of mixed sizes (16-200 stations, 64-2048 timesteps,
           8-64 channels, 1024^2-8192^2 grids) served with continuous batching
+  imaging the uv-grid -> image FFT of the cycle's grid (idg_grid_fft), timed
+          separately, with its HBM rate
 
 --impl reference times that CPU implementation alone (rank 0) on the same
 workload and metric.
@@ -357,6 +359,24 @@ def run_ours(args, rank, world, local_rank):
     if plan is not None:
         plan.close()
 
+    # imaging step around the cycle: the uv-grid -> image FFT (idg_grid_fft) on
+    # this grid, outside the timed cycle; 4 HBM passes (2 row FFTs, 2 transposes)
+    imaging = None
+    if G <= 8192 and (G & (G - 1)) == 0:
+        ge = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        with torch.cuda.stream(stream):
+            ops.grid_fft(gs, grid, -1, stream=stream)  # warm (twiddle table)
+            ge[0].record(stream)
+            for _ in range(3):
+                ops.grid_fft(gs, grid, -1, stream=stream)
+            ge[1].record(stream)
+        stream.synchronize()
+        fft_ms = ge[0].elapsed_time(ge[1]) / 3
+        nbytes = 4 * 2 * grid.numel() * 8
+        imaging = {"grid_fft_ms": fft_ms, "grid": f"1x4x{G}^2",
+                   "hbm_bytes": nbytes, "achieved_gbs": nbytes / (fft_ms * 1e-3) / 1e9,
+                   "note": "not part of the timed cycle; HBM bytes = 4 passes x (read + write) of the grid"}
+
     # plain form (one step, same data) for the batched / plain ratio
     plain = None
     if not args.no_plain and variant != ops.VARIANT_PLAIN:
@@ -443,6 +463,7 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "plain": plain,
         "serving": serving,
+        "imaging": imaging,
         "clocks": clock_info,
     }
 
