@@ -347,8 +347,8 @@ def run_ours(args, rank, world, local_rank):
         "traffic": per_kernel[dom]["traffic"],
         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the first 8192 "
                           "subgrids of this plan, scaled by subgrids (the kernels stream each subgrid's data once)",
-        "peak_source": "measured in this run: FFMA microbenchmark idg_measure_fp32_peak (no FP32 FMA figure "
-                       "is provided by MEASURED_PEAKS.json); the SFU bound (16 sin/cos per SM clock, 2 per "
+        "peak_source": "measured in this run: FFMA microbenchmark idg_measure_fp32_peak (MEASURED_PEAKS.json "
+                       "carries HBM and bf16 figures, no FP32 FMA figure); the SFU bound (16 sin/cos per SM clock, 2 per "
                        "pixel-visibility) is within 2% of the FMA bound on GB300",
         "algorithmic": "34 flop (17 FMA) + 1 sincos per pixel-visibility; %.3g pixel-visibilities per launch" % pixvis,
         "gridder": per_kernel["gridder"],
@@ -373,8 +373,16 @@ def run_ours(args, rank, world, local_rank):
         stream.synchronize()
         fft_ms = ge[0].elapsed_time(ge[1]) / 3
         nbytes = 4 * 2 * grid.numel() * 8
+        hbm_peak = None
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                hbm_peak = float(json.load(f)["hbm_gbs"])
+        except (OSError, ValueError, KeyError):
+            pass
+        ach = nbytes / (fft_ms * 1e-3) / 1e9
         imaging = {"grid_fft_ms": fft_ms, "grid": f"1x4x{G}^2",
-                   "hbm_bytes": nbytes, "achieved_gbs": nbytes / (fft_ms * 1e-3) / 1e9,
+                   "hbm_bytes": nbytes, "achieved_gbs": ach,
+                   "frac_of_measured_hbm": ach / hbm_peak if hbm_peak else None,
                    "note": "not part of the timed cycle; HBM bytes = 4 passes x (read + write) of the grid"}
 
     # plain form (one step, same data) for the batched / plain ratio

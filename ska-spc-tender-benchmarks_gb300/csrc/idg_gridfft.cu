@@ -15,7 +15,8 @@
 // row FFT runs in one CTA: the row is staged in shared memory and transformed
 // by radix-4 Stockham stages (plus one radix-2 stage when log2 G is odd),
 // ping-ponging between two shared buffers; twiddles come from a table of
-// e^{-2 pi i m / G} computed in FP64 on the host.  All passes are HBM-bound:
+// e^{-2 pi i m / G} computed in FP64 on the host and staged in shared memory
+// with the row.  All passes are HBM-bound:
 // 16 bytes per complex cell per pass (read + write).
 #include <cmath>
 #include <map>
@@ -36,37 +37,51 @@ constexpr int kTile = 32;
 __device__ __forceinline__ float2 cm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
-// One FFT over each row (length G, row stride G) of the CTA's row.  DIR = -1
+// One FFT over the CTA's row (length G = 2^LOGG, row stride G).  DIR = -1
 // uses e^{-2 pi i ...}, DIR = +1 its conjugate.  Element i of the row is
 // multiplied by (-1)^i before and after the transform (the centre shifts of
 // this dimension), and by corr[i] (when given) after it for DIR = -1 or before
-// it for DIR = +1.
-template <int DIR>
-__global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data, int G, int logG, const float2 *tw,
+// it for DIR = +1.  The row and the twiddle table are staged in shared memory
+// with all of a thread's 16-byte loads issued before any is used.
+template <int DIR, int LOGG>
+__global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data, const float2 *tw_g,
                                                                    const float *corr) {
+    constexpr int G = 1 << LOGG, kVec = G / 2;  // float4 per row
+    constexpr int kPer = (kVec + kRowThreads - 1) / kRowThreads;
     extern __shared__ float2 sm[];
-    float2 *A = sm, *B = sm + G;
+    float2 *A = sm, *B = sm + G, *tw = sm + 2 * G;
     const int row = blockIdx.x;
     float2 *p = data + (int64_t)row * G;
-    // load (16-byte accesses), pre-multiply for the image -> uv direction
-    for (int i2 = threadIdx.x; i2 < G / 2; i2 += kRowThreads) {
-        const float4 v = reinterpret_cast<const float4 *>(p)[i2];
-        float2 a = make_float2(v.x, v.y), b = make_float2(v.z, v.w);
+    float4 v[kPer], t[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const int i2 = threadIdx.x + k * kRowThreads;
+        if (i2 < kVec) {
+            v[k] = reinterpret_cast<const float4 *>(p)[i2];
+            t[k] = reinterpret_cast<const float4 *>(tw_g)[i2];
+        }
+    }
+    // pre-multiply for the image -> uv direction
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const int i2 = threadIdx.x + k * kRowThreads;
+        if (i2 >= kVec) continue;
         float fa = 1.f, fb = -1.f; // (-1)^i for i = 2 i2, 2 i2 + 1
         if (DIR > 0 && corr) {
             fa *= corr[2 * i2];
             fb *= corr[2 * i2 + 1];
         }
-        A[2 * i2] = make_float2(a.x * fa, a.y * fa);
-        A[2 * i2 + 1] = make_float2(b.x * fb, b.y * fb);
+        A[2 * i2] = make_float2(v[k].x * fa, v[k].y * fa);
+        A[2 * i2 + 1] = make_float2(v[k].z * fb, v[k].w * fb);
+        reinterpret_cast<float4 *>(tw)[i2] = t[k];
     }
     __syncthreads();
-    // Stockham stages: after a stage of radix R over sub-length L (L = product of
-    // the radices done so far), element (k, j) of the output holds the DFT of
-    // length L*R.  Indexing: n = G / (L*R) groups.
+    // Stockham stages: a stage of radix R over sub-length L (the product of the
+    // radices done so far) leaves, in dst, the DFTs of length L*R.
     int L = 1;
     float2 *src = A, *dst = B;
-    const int stages4 = logG / 2, has2 = logG & 1;
+    constexpr int stages4 = LOGG / 2, has2 = LOGG & 1;
+#pragma unroll
     for (int st = 0; st < stages4 + has2; ++st) {
         const int R = (st < stages4) ? 4 : 2;
         const int LR = L * R, n = G / LR;
@@ -78,14 +93,13 @@ __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data,
 #pragma unroll
             for (int r = 0; r < 4; ++r)
                 if (r < R) x[r] = src[b + r * (G / R)];
-            // twiddle for element r: w^(r*k) with w = e^{-2 pi i / LR}
+            // twiddle for element r: e^{-2 pi i r k / LR} = tw[r k n]
             if (k > 0) {
 #pragma unroll
                 for (int r = 1; r < 4; ++r)
                     if (r < R) {
-                        const int m = (r * k) * n; // e^{-2 pi i r k / LR} = tw[r k n]
-                        const float2 w = DIR < 0 ? tw[m] : conjf2(tw[m]);
-                        x[r] = cm(x[r], w);
+                        const float2 w = tw[(r * k) * n];
+                        x[r] = cm(x[r], DIR < 0 ? w : conjf2(w));
                     }
             }
             float2 y[4];
@@ -110,20 +124,48 @@ __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data,
                 if (r < R) dst[q * LR + k + r * L] = y[r];
         }
         __syncthreads();
-        float2 *t = src;
+        float2 *tmp = src;
         src = dst;
-        dst = t;
+        dst = tmp;
         L = LR;
     }
     // post-multiply for the uv -> image direction, store
-    for (int i2 = threadIdx.x; i2 < G / 2; i2 += kRowThreads) {
-        float2 a = src[2 * i2], b = src[2 * i2 + 1];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const int i2 = threadIdx.x + k * kRowThreads;
+        if (i2 >= kVec) continue;
+        const float2 a = src[2 * i2], b = src[2 * i2 + 1];
         float fa = 1.f, fb = -1.f;
         if (DIR < 0 && corr) {
             fa *= corr[2 * i2];
             fb *= corr[2 * i2 + 1];
         }
         reinterpret_cast<float4 *>(p)[i2] = make_float4(a.x * fa, a.y * fa, b.x * fb, b.y * fb);
+    }
+}
+
+template <int DIR, int LOGG>
+cudaError_t row_pass(float2 *grid, int64_t rows, const float2 *tw, const float *corr, cudaStream_t st) {
+    const size_t smem = 3 * sizeof(float2) * ((size_t)1 << LOGG);
+    cudaError_t e = cudaFuncSetAttribute(grid_row_fft_kernel<DIR, LOGG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    grid_row_fft_kernel<DIR, LOGG><<<(unsigned)rows, kRowThreads, smem, st>>>(grid, tw, corr);
+    return cudaGetLastError();
+}
+
+template <int DIR>
+cudaError_t row_pass_g(int logG, float2 *grid, int64_t rows, const float2 *tw, const float *corr, cudaStream_t st) {
+    switch (logG) {
+    case 6: return row_pass<DIR, 6>(grid, rows, tw, corr, st);
+    case 7: return row_pass<DIR, 7>(grid, rows, tw, corr, st);
+    case 8: return row_pass<DIR, 8>(grid, rows, tw, corr, st);
+    case 9: return row_pass<DIR, 9>(grid, rows, tw, corr, st);
+    case 10: return row_pass<DIR, 10>(grid, rows, tw, corr, st);
+    case 11: return row_pass<DIR, 11>(grid, rows, tw, corr, st);
+    case 12: return row_pass<DIR, 12>(grid, rows, tw, corr, st);
+    case 13: return row_pass<DIR, 13>(grid, rows, tw, corr, st);
+    default: return cudaErrorInvalidValue;
     }
 }
 
@@ -188,19 +230,10 @@ cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, cons
     if (e != cudaSuccess) return e;
     int logG = 0;
     while ((1 << logG) < G) ++logG;
-    const size_t smem = 2 * sizeof(float2) * (size_t)G;
     const int64_t rows = (int64_t)planes * G;
     auto rowpass = [&]() -> cudaError_t {
-        if (direction < 0) {
-            cudaError_t e2 = cudaFuncSetAttribute(grid_row_fft_kernel<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e2 != cudaSuccess) return e2;
-            grid_row_fft_kernel<-1><<<(unsigned)rows, kRowThreads, smem, st>>>(grid, G, logG, tw, corr);
-        } else {
-            cudaError_t e2 = cudaFuncSetAttribute(grid_row_fft_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e2 != cudaSuccess) return e2;
-            grid_row_fft_kernel<1><<<(unsigned)rows, kRowThreads, smem, st>>>(grid, G, logG, tw, corr);
-        }
-        return cudaGetLastError();
+        return direction < 0 ? row_pass_g<-1>(logG, grid, rows, tw, corr, st)
+                             : row_pass_g<1>(logG, grid, rows, tw, corr, st);
     };
     const dim3 tgrid(G / kTile, G / kTile, planes);
     // rows (x), transpose, rows (y), transpose back
