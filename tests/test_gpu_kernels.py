@@ -311,6 +311,59 @@ def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
     tuning.set_shapes(S, 0, 0)
 
 
+@pytest.mark.parametrize("S", [24, 48, 64])
+def test_every_batched_shape_at_other_subgrid_sizes(oracle_mod, idg, S):
+    """Every launch shape of both batched kernels (pixel-pair and channel-pair
+    degridders included) on an uneven plan with subgrid sizes that need partial
+    pixel passes and channel ranges that are not multiples of the channel group."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops, tuning
+
+    rng = np.random.default_rng(200 + S)
+    G, C, ns = 2048, 20, 5
+    image_size = 0.04
+    spec = D.ObservationSpec(nstations=ns, disk_radius_m=2500.0, ntimesteps=120, timesteps_per_subgrid=120,
+                             nchannels=C, f_start=140e6, f_end=170e6, subgrid_size=S, grid_size=G,
+                             image_size=image_size, aterm_sigma=0.05, seed=S + 1)
+    obs = D.make_observation(spec)
+    N = 8
+    T = rng.integers(4, 16, N)
+    md = np.zeros(N, L.METADATA_DTYPE)
+    md["time_offset"] = np.concatenate([[0], np.cumsum(T)[:-1]])
+    md["nr_timesteps"] = T
+    md["station1"] = rng.integers(0, ns - 1, N)
+    md["station2"] = md["station1"] + 1
+    md["x"] = rng.integers(0, G - S, N)
+    md["y"] = rng.integers(0, G - S, N)
+    lens = rng.choice([3, 8, 13, 20], N)
+    c0 = np.array([rng.integers(0, C - L_ + 1) for L_ in lens])
+    ext = np.zeros(N, L.SUBGRID_EXT_DTYPE)
+    ext["channel_begin"] = c0
+    ext["channel_end"] = c0 + lens
+    rows = int(T.sum())
+    uvw = np.ascontiguousarray(obs.uvw[:rows])
+    vis = (rng.standard_normal((rows, C, 4)) + 1j * rng.standard_normal((rows, C, 4))).astype(np.complex64)
+    sub_in = (rng.standard_normal((N, 4, S, S)) + 1j * rng.standard_normal((N, 4, S, S))).astype(np.complex64)
+    want_g, want_v = _oracle_with_ext(oracle_mod, G, S, ns, image_size, uvw, obs.wavenumbers, vis, obs.taper,
+                                      obs.aterms, md, ext, sub_in)
+    covered = np.zeros((rows, C), bool)
+    for m, e in zip(md, ext):
+        covered[m["time_offset"]:m["time_offset"] + m["nr_timesteps"], e["channel_begin"]:e["channel_end"]] = True
+    sp = spec_for(G, S, C, ns, obs.aterms.shape[0], image_size)
+    ng, nd = tuning.num_shapes()
+    for sh in range(max(ng, nd)):
+        g_sh, d_sh = min(sh, ng - 1), min(sh, nd - 1)
+        tuning.set_shapes(S, g_sh, d_sh)
+        if sh < ng:
+            got = grid_gpu(sp, md, uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, L.VARIANT_BATCHED, ext=ext)
+            check_rel(f"gridder S={S} shape {g_sh}", got, want_g, TOL)
+        vg = degrid_gpu(sp, md, uvw, obs.wavenumbers, sub_in, obs.taper, obs.aterms, rows, L.VARIANT_BATCHED, ext=ext)
+        check_rel(f"degridder S={S} shape {d_sh}", vg[covered], want_v[covered], TOL)
+        assert np.all(vg[~covered] == 0)
+    assert ops.device_status(clear=True) == 0
+    tuning.set_shapes(S, 0, 0)
+
+
 def test_plan_steps_and_graph_cycle_match_direct_calls(oracle_mod, idg):
     """A plan's grid/degrid steps and its captured CUDA-graph cycle reproduce the
     direct entry points; an uneven plan (longest-first work list) stays within tolerance."""
