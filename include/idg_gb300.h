@@ -202,6 +202,40 @@ IDG_API int idg_degrid_visibilities(const idg_params *params, int variant, int64
                                     void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Planner: the subgrid plan from uvw, on the GPU                      */
+/* ------------------------------------------------------------------ */
+typedef struct idg_planner_params {
+    int64_t nr_baselines;   /* rows of baseline b are b*nr_timesteps .. (b+1)*nr_timesteps-1 */
+    int32_t nr_timesteps;   /* per baseline */
+    int32_t nr_channels;
+    int32_t subgrid_size;   /* S */
+    int32_t grid_size;      /* G */
+    int32_t max_timesteps;  /* per subgrid */
+    int32_t aterm_interval; /* timesteps per A-term slot; 0 = one slot */
+    int32_t margin;         /* cells of a subgrid kept free for the taper; usable width S - margin */
+    int32_t reserved;
+    double image_size;      /* radians */
+} idg_planner_params;
+/* uvw-driven plan with channel and time splitting: per baseline the channels
+ * are cut into contiguous groups (a group closes before channel c when
+ * reach * (f_c - f_first) > (S - margin) / 2, reach = the baseline's largest
+ * |u| or |v| in cells per Hz); per group the time axis is walked and a
+ * subgrid closed when the uv extent of its samples would exceed S - margin
+ * cells, at max_timesteps, or at an A-term slot boundary; the subgrid's centre
+ * cell sits on the centre of that extent.  Inputs are DEVICE arrays: uvw
+ * [nr_baselines * nr_timesteps][3] float (metres), frequencies [nr_channels]
+ * double (Hz), baselines [nr_baselines][2] uint32 (stations).  Outputs:
+ * `metadata` and `ext` (DEVICE, capacity max_subgrids) in (baseline, channel
+ * group, time) order, and the count in *nr_subgrids (host); when the plan has
+ * more than max_subgrids entries the call fails with the needed count in
+ * *nr_subgrids.  Synchronises `stream`; allocates its work space with
+ * cudaMallocAsync on `stream`.  The reference's plan is random
+ * (gridding_initialization.cpp:158-182); this has no counterpart there. */
+IDG_API int idg_plan_subgrids(const idg_planner_params *params, const float *uvw, const double *frequencies,
+                              const uint32_t *baselines, int64_t max_subgrids, idg_metadata *metadata,
+                              idg_subgrid_ext *ext, int64_t *nr_subgrids, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* Execution plans (batching form): device-resident plan + CUDA graph  */
 /* ------------------------------------------------------------------ */
 /* A plan keeps a set of subgrids on the device: metadata, channel sidecar, a

@@ -62,6 +62,21 @@ class IdgParams(ctypes.Structure):
     ]
 
 
+class IdgPlannerParams(ctypes.Structure):
+    _fields_ = [
+        ("nr_baselines", ctypes.c_int64),
+        ("nr_timesteps", ctypes.c_int32),
+        ("nr_channels", ctypes.c_int32),
+        ("subgrid_size", ctypes.c_int32),
+        ("grid_size", ctypes.c_int32),
+        ("max_timesteps", ctypes.c_int32),
+        ("aterm_interval", ctypes.c_int32),
+        ("margin", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("image_size", ctypes.c_double),
+    ]
+
+
 class IdgBenchmarkResult(ctypes.Structure):
     _fields_ = [
         ("in_transfer_time", ctypes.c_double),
@@ -180,6 +195,8 @@ _SIGNATURES = {
     "idg_imaging_cycle": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64,
                           ctypes.c_void_p],
     "idg_release_buffers": [],
+    "idg_plan_subgrids": [ctypes.POINTER(IdgPlannerParams), _P, _P, _P, _I64, _P, _P, ctypes.POINTER(ctypes.c_int64),
+                          _P],
     "idg_plan_create": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, ctypes.POINTER(ctypes.c_void_p)],
     "idg_plan_destroy": [_P],
     "idg_plan_set_cta_limit": [_P, _I32],

@@ -210,6 +210,40 @@ def imaging_cycle(spec: GridSpec, metadata: np.ndarray, uvw: np.ndarray, wavenum
             "h2d_bytes": t.h2d_bytes, "d2h_bytes": t.d2h_bytes, "kernel_launches": t.kernel_launches}
 
 
+def plan_subgrids(uvw, frequencies, baselines, nr_timesteps: int, subgrid_size: int, grid_size: int,
+                  image_size: float, max_timesteps: int, aterm_interval: int = 0, margin: int | None = None,
+                  capacity: int | None = None, stream=None):
+    """The uvw-driven plan with channel and time splitting, computed on the GPU
+    (idg_plan_subgrids): uvw [rows, 3] float32, frequencies [C] float64 and
+    baselines [nb, 2] int32/uint32 on the device.  Returns (metadata, ext) as
+    numpy arrays, identical to datasets.plan_subgrids_split on the same inputs."""
+    nb = baselines.shape[0]
+    if uvw.shape != (nb * nr_timesteps, 3) or uvw.dtype != torch.float32 or not uvw.is_cuda:
+        raise ValueError("uvw must be a float32 CUDA tensor [nr_baselines * nr_timesteps, 3]")
+    if frequencies.dtype != torch.float64 or not frequencies.is_cuda:
+        raise ValueError("frequencies must be a float64 CUDA tensor")
+    if baselines.dtype not in (torch.int32,) or not baselines.is_cuda or baselines.shape[1] != 2:
+        raise ValueError("baselines must be an int32 CUDA tensor [nr_baselines, 2]")
+    prm = _lib.IdgPlannerParams(nb, nr_timesteps, frequencies.shape[0], subgrid_size, grid_size, max_timesteps,
+                                aterm_interval, subgrid_size // 4 if margin is None else margin, 0, image_size)
+    n = ctypes.c_int64(0)
+    cap = capacity if capacity is not None else 0
+    if cap == 0:  # counting call: learn the size, then plan into exactly that much
+        rc = _lib.load().idg_plan_subgrids(ctypes.byref(prm), ptr(uvw), ptr(frequencies), ptr(baselines), 0, None,
+                                            None, ctypes.byref(n), _stream_handle(stream))
+        if rc not in (_lib.IDG_OK, _lib.IDG_ERR_INVALID_ARGUMENT) or n.value <= 0:
+            _lib.check(rc)
+        cap = int(n.value)
+    md = torch.empty((cap, 9), dtype=torch.int32, device=uvw.device)
+    ext = torch.empty((cap, 2), dtype=torch.int32, device=uvw.device)
+    _lib.call("idg_plan_subgrids", ctypes.byref(prm), ptr(uvw), ptr(frequencies), ptr(baselines), cap, ptr(md),
+              ptr(ext), ctypes.byref(n), _stream_handle(stream))
+    k = int(n.value)
+    md_np = md[:k].cpu().numpy().copy().view(_lib.METADATA_DTYPE).reshape(-1)
+    ext_np = ext[:k].cpu().numpy().copy().view(_lib.SUBGRID_EXT_DTYPE).reshape(-1)
+    return md_np, ext_np
+
+
 class Plan:
     """A device-resident execution plan (idg_plan_*): metadata, longest-first work
     list and subgrid work space on the device; optional CUDA graph of one cycle."""
