@@ -160,10 +160,15 @@ IDG_API int idg_degridder(const idg_params *params, int variant, int64_t nr_subg
 IDG_API int idg_subgrid_fft(const idg_params *params, int64_t nr_subgrids, int direction,
                             const float *taper, void *subgrids, void *stream);
 
-/* Adder: grid[z][pol][y+j][x+i] += F[s][pol][j][i] for cells inside the grid. */
+/* Adder: grid[z][pol][y+j][x+i] += F[s][pol][j][i] for cells inside the grid.
+ * w-stacking: planes z = 0..W-1 hold w offsets (z + 1/2) w_step; an entry with
+ * -W <= z < 0 (negative w) is added by Hermitian symmetry into plane -z-1 at
+ * the mirrored cell (G - y - j, G - x - i), conjugated, with xy and yx
+ * swapped.  Entries with z outside [-W, W) are skipped. */
 IDG_API int idg_adder(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
                       const void *subgrids, void *grid, void *stream);
-/* Splitter: F[s][pol][j][i] = grid[z][pol][y+j][x+i] (0 outside). */
+/* Splitter: F[s][pol][j][i] = grid[z][pol][y+j][x+i] (0 outside); the
+ * adder's mirror rule for -W <= z < 0. */
 IDG_API int idg_splitter(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
                          const void *grid, void *subgrids, void *stream);
 
@@ -213,8 +218,9 @@ typedef struct idg_planner_params {
     int32_t max_timesteps;  /* per subgrid */
     int32_t aterm_interval; /* timesteps per A-term slot; 0 = one slot */
     int32_t margin;         /* cells of a subgrid kept free for the taper; usable width S - margin */
-    int32_t reserved;
+    int32_t nr_w_planes;    /* W (>= 1); used when w_step > 0 */
     double image_size;      /* radians */
+    double w_step;          /* wavelengths; > 0: w-stacking, 0: every z = 0 */
 } idg_planner_params;
 /* uvw-driven plan with channel and time splitting: per baseline the channels
  * are cut into contiguous groups (a group closes before channel c when
@@ -222,7 +228,9 @@ typedef struct idg_planner_params {
  * |u| or |v| in cells per Hz); per group the time axis is walked and a
  * subgrid closed when the uv extent of its samples would exceed S - margin
  * cells, at max_timesteps, or at an A-term slot boundary; the subgrid's centre
- * cell sits on the centre of that extent.  Inputs are DEVICE arrays: uvw
+ * cell sits on the centre of that extent; with w_step > 0 its w-plane is
+ * z = floor(w_mid / w_step) (w_mid: centre of its w extent in wavelengths),
+ * clipped to [-W, W-1], negative z being the adder's mirrored planes.  Inputs are DEVICE arrays: uvw
  * [nr_baselines * nr_timesteps][3] float (metres), frequencies [nr_channels]
  * double (Hz), baselines [nr_baselines][2] uint32 (stations).  Outputs:
  * `metadata` and `ext` (DEVICE, capacity max_subgrids) in (baseline, channel

@@ -457,24 +457,45 @@ void oracle_subgrid_dft_f64(int nr_subgrids, int S, int direction, const float *
 /* ------------------------------------------------------------------ */
 /* Adder / splitter                                                   */
 /* ------------------------------------------------------------------ */
+/* Grid cell of subgrid cell (j, i) of an entry: plane, polarisation, row,
+ * column and the conjugation flag.  z in [0, W): direct.  z in [-W, 0): the
+ * Hermitian mirror -- plane -z-1, cell (G - gy, G - gx), xy <-> yx, conjugate.
+ * Returns 0 when the cell (or the entry's plane) is outside the grid. */
+static int oracle_grid_cell(const oracle_metadata *md, int G, int W, int pol, int j, int i, long *plane, int *gpol,
+                            long *gy, long *gx, int *conj) {
+    if (md->z >= 0 && md->z < W) {
+        *plane = md->z;
+        *gpol = pol;
+        *gy = (long)md->y + j;
+        *gx = (long)md->x + i;
+        *conj = 0;
+    } else if (md->z < 0 && md->z >= -W) {
+        *plane = -(long)md->z - 1;
+        *gpol = (pol == 1 || pol == 2) ? 3 - pol : pol;
+        *gy = (long)G - ((long)md->y + j);
+        *gx = (long)G - ((long)md->x + i);
+        *conj = 1;
+    } else {
+        return 0;
+    }
+    return *gy >= 0 && *gy < G && *gx >= 0 && *gx < G;
+}
+
 void oracle_adder_f64(int nr_subgrids, int S, int G, int W, const oracle_metadata *metadata,
                       const double *subgrids, double *grid) {
     for (int s = 0; s < nr_subgrids; ++s) {
         const oracle_metadata md = metadata[s];
-        if (md.z < 0 || md.z >= W) continue;
         for (int pol = 0; pol < 4; ++pol)
-            for (int j = 0; j < S; ++j) {
-                const long gy = (long)md.y + j;
-                if (gy < 0 || gy >= G) continue;
+            for (int j = 0; j < S; ++j)
                 for (int i = 0; i < S; ++i) {
-                    const long gx = (long)md.x + i;
-                    if (gx < 0 || gx >= G) continue;
+                    long plane, gy, gx;
+                    int gpol, cj;
+                    if (!oracle_grid_cell(&md, G, W, pol, j, i, &plane, &gpol, &gy, &gx, &cj)) continue;
                     const size_t src = ((((size_t)s * 4 + pol) * S + j) * S + i) * 2;
-                    const size_t dst = (((((size_t)md.z * 4 + pol) * G) + gy) * G + gx) * 2;
+                    const size_t dst = (((((size_t)plane * 4 + gpol) * G) + gy) * G + gx) * 2;
                     grid[dst] += subgrids[src];
-                    grid[dst + 1] += subgrids[src + 1];
+                    grid[dst + 1] += cj ? -subgrids[src + 1] : subgrids[src + 1];
                 }
-            }
     }
 }
 
@@ -485,16 +506,17 @@ void oracle_splitter_f64(int nr_subgrids, int S, int G, int W, const oracle_meta
         for (int pol = 0; pol < 4; ++pol)
             for (int j = 0; j < S; ++j)
                 for (int i = 0; i < S; ++i) {
-                    const long gy = (long)md.y + j, gx = (long)md.x + i;
                     const size_t dst = ((((size_t)s * 4 + pol) * S + j) * S + i) * 2;
-                    if (md.z < 0 || md.z >= W || gy < 0 || gy >= G || gx < 0 || gx >= G) {
+                    long plane, gy, gx;
+                    int gpol, cj;
+                    if (!oracle_grid_cell(&md, G, W, pol, j, i, &plane, &gpol, &gy, &gx, &cj)) {
                         subgrids[dst] = 0;
                         subgrids[dst + 1] = 0;
                         continue;
                     }
-                    const size_t src = (((((size_t)md.z * 4 + pol) * G) + gy) * G + gx) * 2;
+                    const size_t src = (((((size_t)plane * 4 + gpol) * G) + gy) * G + gx) * 2;
                     subgrids[dst] = grid[src];
-                    subgrids[dst + 1] = grid[src + 1];
+                    subgrids[dst + 1] = cj ? -grid[src + 1] : grid[src + 1];
                 }
     }
 }

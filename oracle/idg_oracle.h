@@ -90,11 +90,14 @@ void oracle_subgrid_dft_f64(int nr_subgrids, int subgrid_size, int direction, co
 
 /* Adder: grid[z][pol][y0+j][x0+i] += F[s][pol][j][i] for every cell inside
  * the G x G grid (cells outside are dropped), in subgrid order; z is the
- * metadata w-plane index (subgrids with z outside [0, nr_w_planes) are
- * skipped).  grid is complex double [W][4][G][G]. */
+ * metadata w-plane index.  An entry with -W <= z < 0 (negative w) adds
+ * conj(F) to plane -z-1 at the mirrored cell (G - y0 - j, G - x0 - i) with
+ * xy and yx swapped (Hermitian symmetry); entries with z outside [-W, W) are
+ * skipped.  grid is complex double [W][4][G][G]. */
 void oracle_adder_f64(int nr_subgrids, int subgrid_size, int grid_size, int nr_w_planes,
                       const oracle_metadata *metadata, const double *subgrids, double *grid);
-/* Splitter: F[s][pol][j][i] = grid[z][pol][y0+j][x0+i], 0 outside. */
+/* Splitter: F[s][pol][j][i] = grid[z][pol][y0+j][x0+i], 0 outside; the
+ * adder's mirror rule for -W <= z < 0 (conjugated read of the mirrored cell). */
 void oracle_splitter_f64(int nr_subgrids, int subgrid_size, int grid_size, int nr_w_planes,
                          const oracle_metadata *metadata, const double *grid, double *subgrids);
 

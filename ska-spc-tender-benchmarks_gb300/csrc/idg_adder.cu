@@ -2,7 +2,15 @@
 //
 // Adder   : grid[z][pol][y0+j][x0+i] += F[s][pol][j][i]   for cells inside the G x G grid
 // Splitter: F[s][pol][j][i] = grid[z][pol][y0+j][x0+i]     (0 for cells outside)
-// (x0, y0, z) are the plan entry's coordinate.  Both are bandwidth kernels:
+// (x0, y0, z) are the plan entry's coordinate.  w-stacking with negative w:
+// the grid holds w-planes z = 0 .. W-1 (offsets (z + 1/2) w_step >= 0); an
+// entry with -W <= z < 0 uses the Hermitian symmetry V(-u,-v,-w) = V(u,v,w)^H
+// and goes to plane -z-1 at the mirrored cell (G - gy, G - gx), conjugated,
+// with the cross-hand correlations swapped (xy <-> yx):
+//   adder    grid[-z-1][pol'][G-gy][G-gx] += conj(F[s][pol][j][i])
+//   splitter F[s][pol][j][i] = conj(grid[-z-1][pol'][G-gy][G-gx])
+// (gy = y0 + j, gx = x0 + i, pol' = the swapped index; mirrored cells outside
+// the grid are skipped / read as 0).  Both are bandwidth kernels:
 // one CTA per subgrid, consecutive threads on consecutive cells of a row, so
 // subgrid and grid accesses coalesce.  Subgrid footprints of one plan overlap
 // (consecutive time slices of a baseline land on nearly the same cells), so
@@ -22,9 +30,21 @@ __global__ void __launch_bounds__(kThreads) adder_kernel(const idg_metadata *md,
                                                          const float2 *subgrids, float2 *grid) {
     const int s = blockIdx.x;
     const idg_metadata m = md[s];
-    if (m.z < 0 || m.z >= W) return;
+    if (m.z < -W || m.z >= W) return;
     const int64_t S2 = (int64_t)S * S;
     const float2 *src = subgrids + (int64_t)s * 4 * S2;
+    if (m.z < 0) { // mirrored into plane -z-1
+        float2 *mp = grid + (int64_t)(-m.z - 1) * 4 * G * G;
+        for (int e = threadIdx.x; e < 4 * S * S; e += kThreads) {
+            const int pol = e / (S * S), r = e - pol * S * S, j = r / S, i = r - j * S;
+            const int gy = G - (m.y + j), gx = G - (m.x + i);
+            if (gy < 0 || gy >= G || gx < 0 || gx >= G) continue;
+            const int pm = (pol == 1 || pol == 2) ? 3 - pol : pol;
+            const float2 v = src[pol * S2 + r];
+            atomicAdd(mp + ((int64_t)pm * G + gy) * G + gx, make_float2(v.x, -v.y));
+        }
+        return;
+    }
     float2 *plane0 = grid + (int64_t)m.z * 4 * G * G;
     if ((m.x & 1) == 0 && (S & 1) == 0 && (G & 1) == 0) {
         // two cells per thread, 16-byte aligned on both sides (even x, S and G)
@@ -60,13 +80,16 @@ __global__ void __launch_bounds__(kThreads) splitter_kernel(const idg_metadata *
     const idg_metadata m = md[s];
     const int64_t S2 = (int64_t)S * S;
     float2 *dst = subgrids + (int64_t)s * 4 * S2;
-    const bool plane_ok = m.z >= 0 && m.z < W;
-    const float2 *plane0 = grid + (int64_t)(plane_ok ? m.z : 0) * 4 * G * G;
+    const bool plane_ok = m.z >= -W && m.z < W;
+    const bool mirror = m.z < 0;
+    const float2 *plane0 = grid + (int64_t)(plane_ok ? (mirror ? -m.z - 1 : m.z) : 0) * 4 * G * G;
     for (int e = threadIdx.x; e < 4 * S * S; e += kThreads) {
         const int pol = e / (S * S), r = e - pol * S * S, j = r / S, i = r - j * S;
-        const int gy = m.y + j, gx = m.x + i;
+        const int gy = mirror ? G - (m.y + j) : m.y + j, gx = mirror ? G - (m.x + i) : m.x + i;
+        const int pg = (mirror && (pol == 1 || pol == 2)) ? 3 - pol : pol;
         float2 v = make_float2(0.f, 0.f);
-        if (plane_ok && gy >= 0 && gy < G && gx >= 0 && gx < G) v = plane0[((int64_t)pol * G + gy) * G + gx];
+        if (plane_ok && gy >= 0 && gy < G && gx >= 0 && gx < G) v = plane0[((int64_t)pg * G + gy) * G + gx];
+        if (mirror) v.y = -v.y;
         dst[e] = v;
     }
 }

@@ -26,8 +26,8 @@ namespace {
 
 struct PlanArgs {
     int64_t nb;
-    int nt, C, S, G, tmax, ai, width;
-    double scale;
+    int nt, C, S, G, tmax, ai, width, W;
+    double scale, w_step;
     const float *uvw;        // [nb * nt][3]
     const double *f;         // [C] Hz
     const uint32_t *bl;      // [nb][2]
@@ -38,6 +38,8 @@ struct PlanArgs {
     idg_metadata *md;
     idg_subgrid_ext *ext;
 };
+
+constexpr double kSpeedOfLight = 299792458.0;
 
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
@@ -113,6 +115,7 @@ __global__ void plan_walk_kernel(PlanArgs a) {
         n = max(n, 1);
         if (WRITE) {
             double lu_min = INFINITY, hu_max = -INFINITY, lv_min = INFINITY, hv_max = -INFINITY;
+            double lw_min = INFINITY, hw_max = -INFINITY;
             for (int t = t0; t < t0 + n; ++t) {
                 double lu, hu, lv, hv;
                 bounds(rows + 3 * t, fa, fb, a.scale, lu, hu, lv, hv);
@@ -120,6 +123,15 @@ __global__ void plan_walk_kernel(PlanArgs a) {
                 hu_max = fmax(hu_max, hu);
                 lv_min = fmin(lv_min, lv);
                 hv_max = fmax(hv_max, hv);
+                const double w = rows[3 * t + 2];
+                const double wa = __ddiv_rn(mul(w, fa), kSpeedOfLight), wb = __ddiv_rn(mul(w, fb), kSpeedOfLight);
+                lw_min = fmin(lw_min, fmin(wa, wb));
+                hw_max = fmax(hw_max, fmax(wa, wb));
+            }
+            int z = 0;
+            if (a.w_step > 0.0) {
+                const double zf = floor(__ddiv_rn(mul(0.5, add(lw_min, hw_max)), a.w_step));
+                z = (int)fmin(fmax(zf, (double)-a.W), (double)(a.W - 1));
             }
             const double mid_u = mul(0.5, add(lu_min, hu_max)), mid_v = mul(0.5, add(lv_min, hv_max));
             const double hg = 0.5 * (double)a.G, hs = 0.5 * (double)a.S;
@@ -132,7 +144,7 @@ __global__ void plan_walk_kernel(PlanArgs a) {
             m.station2 = a.bl[2 * b + 1];
             m.x = (int32_t)floor(add(sub(add(mid_u, hg), hs), 0.5));
             m.y = (int32_t)floor(add(sub(add(mid_v, hg), hs), 0.5));
-            m.z = 0;
+            m.z = z;
             a.md[out] = m;
             a.ext[out] = idg_subgrid_ext{c0, c1};
             ++out;
@@ -154,7 +166,7 @@ IDG_API int idg_plan_subgrids(const idg_planner_params *p, const float *uvw, con
     *nr_subgrids = 0;
     if (p->nr_baselines < 1 || p->nr_timesteps < 1 || p->nr_channels < 1 || p->subgrid_size < 2 ||
         p->grid_size < p->subgrid_size || p->max_timesteps < 1 || p->aterm_interval < 0 || p->margin < 0 ||
-        p->margin >= p->subgrid_size || !(p->image_size > 0.0))
+        p->margin >= p->subgrid_size || !(p->image_size > 0.0) || !(p->w_step >= 0.0) || p->nr_w_planes < 1)
         return fail(IDG_ERR_INVALID_ARGUMENT, "planner parameters out of range");
     if ((int64_t)p->nr_baselines * p->nr_timesteps > INT32_MAX)
         return fail(IDG_ERR_INVALID_ARGUMENT, "more than 2^31 rows");
@@ -170,7 +182,9 @@ IDG_API int idg_plan_subgrids(const idg_planner_params *p, const float *uvw, con
     a.tmax = p->max_timesteps;
     a.ai = p->aterm_interval;
     a.width = p->subgrid_size - p->margin;
-    a.scale = p->image_size / 299792458.0;
+    a.scale = p->image_size / kSpeedOfLight;
+    a.w_step = p->w_step;
+    a.W = p->nr_w_planes;
     a.uvw = uvw;
     a.f = frequencies;
     a.bl = baselines;

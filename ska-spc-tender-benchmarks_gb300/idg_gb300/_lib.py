@@ -72,8 +72,9 @@ class IdgPlannerParams(ctypes.Structure):
         ("max_timesteps", ctypes.c_int32),
         ("aterm_interval", ctypes.c_int32),
         ("margin", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("nr_w_planes", ctypes.c_int32),
         ("image_size", ctypes.c_double),
+        ("w_step", ctypes.c_double),
     ]
 
 

@@ -63,6 +63,7 @@ class ObservationSpec:
     seed: int = 1234
     taper_c: float = 3.0 * np.pi
     subgrid_limit: int = 0     # > 0: only the plan's first subgrid_limit subgrids (and their rows) are used
+    nr_w_planes: int = 1       # w-stacking (split plans, w_step > 0): planes 0..W-1, negative w mirrored
 
     @property
     def n_baselines(self) -> int:
@@ -210,7 +211,13 @@ def plan_subgrids_split(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.
     is placed as in ``plan_subgrids`` (centre cell on the centre of the extent).
     Returns (metadata METADATA_DTYPE[N], ext SUBGRID_EXT_DTYPE[N] with the
     channel range [channel_begin, channel_end) of each subgrid).  Every
-    (baseline, timestep, channel) sample belongs to exactly one subgrid."""
+    (baseline, timestep, channel) sample belongs to exactly one subgrid.
+
+    w-stacking (spec.w_step > 0): a subgrid's w-plane index is
+    z = floor(w_mid / w_step), w_mid the centre of its samples' w extent in
+    wavelengths, clipped to [-W, W-1] (W = spec.nr_w_planes); negative z are the
+    mirrored planes of the adder.  w_step is taken at float32 precision, as
+    the kernels see it."""
     from ._lib import SUBGRID_EXT_DTYPE
 
     nb, nt = spec.n_baselines, spec.ntimesteps
@@ -219,10 +226,13 @@ def plan_subgrids_split(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.
     tmax = spec.timesteps_per_subgrid
     f = np.asarray(frequencies, np.float64)
     scale = img / SPEED_OF_LIGHT  # cells per (metre * Hz)
+    w_step = float(np.float32(spec.w_step))
+    W = spec.nr_w_planes
     rows_md, rows_ext = [], []
     for b in range(nb):
         u = uvw[b * nt:(b + 1) * nt, 0].astype(np.float64)
         v = uvw[b * nt:(b + 1) * nt, 1].astype(np.float64)
+        w = uvw[b * nt:(b + 1) * nt, 2].astype(np.float64)
         reach = max(np.abs(u).max(), np.abs(v).max()) * scale
         # channel groups
         groups, c0 = [], 0
@@ -235,6 +245,8 @@ def plan_subgrids_split(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.
             ua, ub, va, vb = u * fa * scale, u * fb * scale, v * fa * scale, v * fb * scale
             lo_u, hi_u = np.minimum(ua, ub), np.maximum(ua, ub)
             lo_v, hi_v = np.minimum(va, vb), np.maximum(va, vb)
+            wa, wb = w * fa / SPEED_OF_LIGHT, w * fb / SPEED_OF_LIGHT
+            lo_w, hi_w = np.minimum(wa, wb), np.maximum(wa, wb)
             t0 = 0
             while t0 < nt:
                 t1 = min(nt, t0 + tmax)
@@ -249,10 +261,14 @@ def plan_subgrids_split(spec: ObservationSpec, uvw: np.ndarray, frequencies: np.
                 s = slice(t0, t0 + n)
                 mid_u = 0.5 * (lo_u[s].min() + hi_u[s].max())
                 mid_v = 0.5 * (lo_v[s].min() + hi_v[s].max())
+                z = 0
+                if w_step > 0:
+                    mid_w = 0.5 * (lo_w[s].min() + hi_w[s].max())
+                    z = int(min(max(np.floor(mid_w / w_step), -W), W - 1))
                 rows_md.append((0, b * nt + t0, n, t0 // spec.aterm_interval if spec.aterm_interval > 0 else 0,
                                 baselines[b, 0], baselines[b, 1],
                                 int(np.floor(mid_u + G / 2 - S / 2 + 0.5)), int(np.floor(mid_v + G / 2 - S / 2 + 0.5)),
-                                0))
+                                z))
                 rows_ext.append((c0, c1))
                 t0 += n
     md = np.array(rows_md, dtype=METADATA_DTYPE)

@@ -212,7 +212,7 @@ def imaging_cycle(spec: GridSpec, metadata: np.ndarray, uvw: np.ndarray, wavenum
 
 def plan_subgrids(uvw, frequencies, baselines, nr_timesteps: int, subgrid_size: int, grid_size: int,
                   image_size: float, max_timesteps: int, aterm_interval: int = 0, margin: int | None = None,
-                  capacity: int | None = None, stream=None):
+                  capacity: int | None = None, w_step: float = 0.0, nr_w_planes: int = 1, stream=None):
     """The uvw-driven plan with channel and time splitting, computed on the GPU
     (idg_plan_subgrids): uvw [rows, 3] float32, frequencies [C] float64 and
     baselines [nb, 2] int32/uint32 on the device.  Returns (metadata, ext) as
@@ -225,7 +225,8 @@ def plan_subgrids(uvw, frequencies, baselines, nr_timesteps: int, subgrid_size: 
     if baselines.dtype not in (torch.int32,) or not baselines.is_cuda or baselines.shape[1] != 2:
         raise ValueError("baselines must be an int32 CUDA tensor [nr_baselines, 2]")
     prm = _lib.IdgPlannerParams(nb, nr_timesteps, frequencies.shape[0], subgrid_size, grid_size, max_timesteps,
-                                aterm_interval, subgrid_size // 4 if margin is None else margin, 0, image_size)
+                                aterm_interval, subgrid_size // 4 if margin is None else margin, nr_w_planes,
+                                image_size, float(np.float32(w_step)))
     n = ctypes.c_int64(0)
     cap = capacity if capacity is not None else 0
     if cap == 0:  # counting call: learn the size, then plan into exactly that much

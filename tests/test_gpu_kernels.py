@@ -140,6 +140,8 @@ def test_subgrid_fft_vs_dft(oracle_mod, idg, S):
 
 
 def test_adder_splitter_vs_oracle(oracle_mod, idg):
+    """Adder and splitter with w-planes, negative-w entries (mirrored, conjugated)
+    and entries outside the planes or partly outside the grid."""
     from idg_gb300 import ops
 
     S, G, W = 16, 96, 2
@@ -148,8 +150,10 @@ def test_adder_splitter_vs_oracle(oracle_mod, idg):
     md = np.zeros(N, L.METADATA_DTYPE)
     md["x"] = rng.integers(-S + 2, G - 2, N)
     md["y"] = rng.integers(-S + 2, G - 2, N)
-    md["z"] = rng.integers(0, W, N)
+    md["z"] = rng.integers(-W, W, N)  # negative z: Hermitian mirror into plane -z-1
     md["z"][0] = 5  # outside the w-planes: skipped by the adder, zeros from the splitter
+    md["z"][1] = -W - 1
+    assert (md["z"] < 0).sum() >= 8
     sub = (rng.standard_normal((N, 4, S, S)) + 1j * rng.standard_normal((N, 4, S, S))).astype(np.complex64)
     sp = spec_for(G, S, 1, 2, 1, 0.05, W=W)
     grid = torch.zeros((W, 4, G, G), dtype=torch.complex64, device="cuda")

@@ -157,3 +157,32 @@ def test_split_plan_covers_every_sample_once_and_fits(idg, S):
     assert np.all(md["nr_timesteps"] <= spec.timesteps_per_subgrid)
     again = D.make_observation(spec, split=True)
     assert np.array_equal(again.metadata, md) and np.array_equal(again.ext, ext)
+
+
+def test_split_plan_w_planes(idg):
+    """w-stacking in the split planner: each subgrid's z is floor(w_mid / w_step),
+    w_mid the centre of the w extent (wavelengths) of all its samples, clipped
+    to [-W, W-1]; both signs occur; w_step = 0 leaves every z at 0 and the rest
+    of the plan unchanged."""
+    import dataclasses
+
+    from idg_gb300 import datasets as D
+
+    spec = D.ObservationSpec(nstations=8, disk_radius_m=2500.0, ntimesteps=256, timesteps_per_subgrid=64,
+                             nchannels=16, f_start=140e6, f_end=170e6, subgrid_size=32, grid_size=512,
+                             image_size=0.04, w_step=300.0, nr_w_planes=4, aterm_interval=128, dec_deg=20.0, seed=5)
+    obs = D.make_observation(spec, split=True)
+    md, ext = obs.metadata, obs.ext
+    W, w_step = spec.nr_w_planes, float(np.float32(spec.w_step))
+    f = obs.frequencies.astype(np.float64)
+    want = np.empty(md.shape[0], np.int64)
+    for i, (m, e) in enumerate(zip(md, ext)):
+        r = slice(int(m["time_offset"]), int(m["time_offset"]) + int(m["nr_timesteps"]))
+        wl = obs.uvw[r, 2].astype(np.float64)[:, None] * f[None, e["channel_begin"]:e["channel_end"]] / D.SPEED_OF_LIGHT
+        want[i] = min(max(np.floor(0.5 * (wl.min() + wl.max()) / w_step), -W), W - 1)
+    assert np.array_equal(md["z"], want)
+    assert (md["z"] < 0).any() and (md["z"] >= 0).any()
+    flat = D.make_observation(dataclasses.replace(spec, w_step=0.0), split=True)
+    assert np.all(flat.metadata["z"] == 0)
+    rest = [n for n in md.dtype.names if n != "z"]
+    assert np.array_equal(flat.metadata[rest], md[rest]) and np.array_equal(flat.ext, ext)
