@@ -19,6 +19,9 @@
 //    When a tile's bound pi + max|kappa| max|Q| stays below kFastBound the
 //    sincos takes x directly (the SFU reduces the argument itself; the error
 //    grows as |x| * 2^-24), otherwise x is reduced to [-pi, pi] first.
+//  * Shapes 15 and 16 replace the per-channel sincos of those tiles by an
+//    exact channel recurrence (grid_tile_recur): the autotuner keeps them
+//    when they are faster on the data at hand.
 #include "idg_device.cuh"
 #include "idg_internal.h"
 #include "idg_ptx.cuh"
@@ -46,7 +49,7 @@ struct SmemHead {
 };
 
 struct Layout {
-    size_t raw, vexp, coef, kappa, geo, total;
+    size_t raw, vexp, coef, kappa, chain, geo, total;
 };
 
 __host__ __device__ inline Layout layout(int S, int C, int tile_vis) {
@@ -57,12 +60,27 @@ __host__ __device__ inline Layout layout(int S, int C, int tile_vis) {
     L.coef = off; off += (size_t)kMaxTT * 48;          // per timestep: (a,a,b,b) (g,g,qu,qu) (qv,qv,qw,qw)
     L.kappa = off; off += (size_t)C * 8;               // (kappa, kappa)
     off = (off + 15) & ~size_t(15);
+    L.chain = off; off += (size_t)C * 16;              // channel chains (recurrence form)
     L.geo = off;  off += (size_t)(S * S / 2) * 24;      // per pair: (hx0,hx1) (hy,hy) (n0,n1)
     L.total = off;
     return L;
 }
 
 __device__ __forceinline__ f2 dup(float v) { return pack2(v, v); }
+__device__ __forceinline__ f2 neg2(f2 v) { return v ^ 0x8000000080000000ull; }
+
+// Channel chain of the recurrence form: channels [c, c + len) of a subgrid
+// whose consecutive wavenumber differences kappa[i+1] - kappa[i] (exact in
+// float) all equal d.  `newd` is set when d differs from the previous chain's
+// (or the chain opens a channel chunk), i.e. when the step factor must be
+// recomputed.
+struct ChainInfo {
+    int len;
+    float d;
+    int newd;
+    int pad;
+};
+constexpr int kMaxChain = 16; // channels per chain at most: the re-anchoring interval
 
 // x - 2 pi rint(x / 2 pi), elementwise on a pair (Cody-Waite, two constants).
 __device__ __forceinline__ f2 reduce_2pi(f2 x) {
@@ -160,6 +178,7 @@ constexpr int kFtz = 2;      // SFU sine/cosine flushing subnormal arguments
 constexpr int kGauss = 4;    // three-multiplication MACs (12 accumulators per pair)
 constexpr int kUnroll2 = 8;  // channel loop unrolled by two
 constexpr int kUnroll4 = 16; // channel loop unrolled by four
+constexpr int kRecur = 32;   // channel recurrence on tiles within the unreduced bound
 
 // One staged tile: tt timesteps x ncc channels.
 // PIPE & kPipe: the channel loop is software pipelined -- the sincos of channel
@@ -208,6 +227,107 @@ __device__ __forceinline__ void grid_tile(f2 (&acc)[PAIRS][NACC], const int (&pr
     }
 }
 
+// Recurrence form of one staged tile (unreduced-bound tiles only, Gauss MACs).
+// The phase of channel c is x_c = tau0 + kappa_c Q, so along a chain of
+// channels whose wavenumbers step by the same d,
+// exp(i x_{c+1}) = exp(i x_c) exp(i d Q).  Per (pixel, timestep, chain): one
+// sincos for the anchor channel, and one for exp(i d Q) when d changed;
+// every other channel costs a complex multiplication on the FMA pipe instead
+// of a sincos on the SFU.  Float wavenumbers of linearly spaced channels step
+// by one of two neighbouring floats, so narrow bands give long chains (16
+// channels over 150-160 MHz: 11 + 5 channels, one step factor); chains are at
+// most kMaxChain long, which bounds the accumulated rounding to a few units in
+// the last place of the phase.
+template <int PAIRS, int UNR, bool FTZ, bool AHEAD>
+__device__ __forceinline__ void grid_tile_recur(f2 (&acc)[PAIRS][12], const int (&pr)[PAIRS], const float4 *coef,
+                                                const f2 *geo, const float4 *vexp, const f2 *kp,
+                                                const ChainInfo *chains, int tt, int ncc) {
+    for (int t = 0; t < tt; ++t) {
+        const float4 c0 = coef[3 * t], c1 = coef[3 * t + 1], c2 = coef[3 * t + 2];
+        const f2 A2 = pack2(c0.x, c0.y), B2 = pack2(c0.z, c0.w), G2 = pack2(c1.x, c1.y);
+        const f2 QU = pack2(c1.z, c1.w), QV = pack2(c2.x, c2.y), QW = pack2(c2.z, c2.w);
+        const float4 *vt = vexp + (size_t)t * ncc * 6;
+        f2 Dc[PAIRS], Ds[PAIRS], Dn[PAIRS];
+        for (int cs = 0; cs < ncc;) {
+            const ChainInfo ch = chains[cs];
+            f2 Rc[PAIRS], Rs[PAIRS];
+#pragma unroll
+            for (int j = 0; j < PAIRS; ++j) {
+                // tau0 and Q per chain (not kept live across the channel loop)
+                const f2 hx = geo[3 * pr[j]], hy = geo[3 * pr[j] + 1], nn = geo[3 * pr[j] + 2];
+                const f2 tau0 = reduce_2pi(ffma2(A2, hx, ffma2(B2, hy, fmul2(G2, nn))));
+                const f2 Q = ffma2(QU, hx, ffma2(QV, hy, fmul2(QW, nn)));
+                sincos_pair<FTZ>(ffma2(kp[cs], Q, tau0), Rc[j], Rs[j]);
+                if (ch.newd) {
+                    sincos_pair<FTZ>(fmul2(dup(ch.d), Q), Dc[j], Ds[j]);
+                    Dn[j] = neg2(Ds[j]);
+                }
+            }
+            const int ce = cs + ch.len;
+#pragma unroll UNR
+            for (int c = cs; c < ce; ++c) {
+                if (AHEAD) {
+                    // next channel's phasor first, so its two dependent FMA levels
+                    // overlap this channel's MACs
+                    f2 nc_[PAIRS], ns_[PAIRS];
+#pragma unroll
+                    for (int j = 0; j < PAIRS; ++j) {
+                        nc_[j] = ffma2(Rc[j], Dc[j], fmul2(Rs[j], Dn[j]));
+                        ns_[j] = ffma2(Rc[j], Ds[j], fmul2(Rs[j], Dc[j]));
+                    }
+                    channel_macs<PAIRS>(acc, vt + 6 * c, Rc, Rs);
+#pragma unroll
+                    for (int j = 0; j < PAIRS; ++j) {
+                        Rc[j] = nc_[j];
+                        Rs[j] = ns_[j];
+                    }
+                } else {
+                    channel_macs<PAIRS>(acc, vt + 6 * c, Rc, Rs);
+#pragma unroll
+                    for (int j = 0; j < PAIRS; ++j) {
+                        const f2 rc = ffma2(Rc[j], Dc[j], fmul2(Rs[j], Dn[j]));
+                        const f2 rs = ffma2(Rc[j], Ds[j], fmul2(Rs[j], Dc[j]));
+                        Rc[j] = rc;
+                        Rs[j] = rs;
+                    }
+                }
+            }
+            cs = ce;
+        }
+    }
+}
+
+// Chains of a subgrid's channels (one thread): maximal runs of equal
+// wavenumber steps, cut at every channel chunk and after max_len channels
+// (max_len <= kMaxChain).
+__device__ inline void build_chains(const f2 *kap, ChainInfo *chains, int nc, int chunk, int max_len) {
+    float hi, dprev = 0.f;
+    int c = 0;
+    while (c < nc) {
+        const int cs = c;
+        const int lim = min(min(nc, (cs / chunk + 1) * chunk), cs + max_len);
+        const bool opens_chunk = cs % chunk == 0;
+        float kprev, d = dprev;
+        unpack2(kap[c], kprev, hi);
+        ++c;
+        if (c < lim) {
+            float kc;
+            unpack2(kap[c], kc, hi);
+            d = kc - kprev;
+            for (++c; c < lim; ++c) {
+                kprev = kc;
+                unpack2(kap[c], kc, hi);
+                if (kc - kprev != d) break;
+            }
+        }
+        // a one-channel chain never steps: it keeps the previous factor
+        const bool newd = opens_chunk || (c - cs > 1 && __float_as_int(d) != __float_as_int(dprev));
+        if (c - cs == 1 && opens_chunk) d = 0.f;
+        chains[cs] = ChainInfo{c - cs, d, newd ? 1 : 0, 0};
+        dprev = d;
+    }
+}
+
 // Kernel shape: NT threads per CTA, PAIRS pixel pairs per thread per pass,
 // TV visibilities per staged tile, at least MINB CTAs per SM (register cap).
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
@@ -215,6 +335,7 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
     constexpr int kT = NT, kPairs = PAIRS, kPassPairs = NT * PAIRS, kTileVis = TV, kMaxChunk = TV;
     constexpr bool kG = (PIPE & kGauss) != 0;
     constexpr int kAcc = kG ? 12 : 8, kUnr = (PIPE & kUnroll4) ? 4 : (PIPE & kUnroll2) ? 2 : 1;
+    constexpr bool kRec = kG && (PIPE & kRecur) != 0;
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = a.S, S2 = S * S, npairs = S2 / 2;
     const Layout L = layout(S, a.C, TV);
@@ -224,6 +345,7 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
     float4 *coef = reinterpret_cast<float4 *>(smem + L.coef);
     f2 *kap = reinterpret_cast<f2 *>(smem + L.kappa);
     f2 *geo = reinterpret_cast<f2 *>(smem + L.geo);
+    ChainInfo *chains = reinterpret_cast<ChainInfo *>(smem + L.chain);
     const int tid = threadIdx.x;
 
     if (tid == 0) {
@@ -277,6 +399,8 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 
         const int chunk = nc < kMaxChunk ? nc : kMaxChunk;
         const int TT = nc > 0 ? min(kMaxTT, kTileVis / chunk) : 1;
+        // read after the staging barrier of the first tile
+        if (kRec && tid == 0) build_chains(kap, chains, nc, chunk, kMaxChain);
         const float hmax = 0.5f * (float)(S - 1);
         const float3 gc = pixel_geometry(0, S, a.image_size);
         const float nmax = gc.z;
@@ -369,7 +493,13 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
                     const bool fast = head->fast != 0;
 
                     // ---- compute
-                    if (fast)
+                    if constexpr (kRec) {
+                        if (fast)
+                            grid_tile_recur<kPairs, kUnr, (PIPE & kFtz) != 0, (PIPE & kPipe) != 0>(acc, pr, coef, geo, vexp, kap + cb,
+                                                                             chains + cb, tt, ncc);
+                        else
+                            grid_tile<kPairs, false, PIPE, kAcc, kUnr>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
+                    } else if (fast)
                         grid_tile<kPairs, true, PIPE, kAcc, kUnr>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
                     else
                         grid_tile<kPairs, false, PIPE, kAcc, kUnr>(acc, pr, coef, geo, vexp, kap + cb, tt, ncc);
@@ -444,6 +574,8 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 //  12: 128 x 3 (384 pairs per pass: whole passes for S = 48), Gauss, pipelined, unrolled by two
 //  13: shape 8 with the channel loop unrolled by four
 //  14: shape 7 with the channel loop unrolled by four
+//  15: 128 x 4, 2 CTAs/SM, Gauss MACs, channel recurrence (chains <= 16), unrolled by four
+//  16: shape 15 with each channel's next phasor computed ahead of its MACs
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -465,7 +597,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return 15; }
+int gridder_fast_shapes() { return 17; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -483,6 +615,8 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 12: return launch_shape<128, 3, 256, 2, kGauss | kPipe | kUnroll2>(a, stream);
     case 13: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll4>(a, stream);
     case 14: return launch_shape<128, 4, 256, 2, kGauss | kUnroll4>(a, stream);
+    case 15: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kUnroll4>(a, stream);
+    case 16: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kPipe | kUnroll4>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }

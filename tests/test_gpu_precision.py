@@ -38,8 +38,9 @@ def _decile_errors(got, want, decile, nd=10):
     return out
 
 
-@pytest.mark.parametrize("S", [32, 64])
-def test_precision_sweep_by_baseline_decile(oracle_mod, idg, S):
+def _sample(oracle_mod, S):
+    """Config-3 observation, a seeded sample of PER_DECILE subgrids per baseline
+    decile, random visibilities / subgrids and the FP64 oracle's outputs."""
     from idg_gb300 import datasets as D
 
     spec = D.config3(S, nstations=12, ntimesteps=512)
@@ -68,6 +69,13 @@ def test_precision_sweep_by_baseline_decile(oracle_mod, idg, S):
         r = slice(int(m["time_offset"]), int(m["time_offset"]) + int(m["nr_timesteps"]))
         covered[r, e["channel_begin"]:e["channel_end"]] = True
         vdec[r, e["channel_begin"]:e["channel_end"]] = d
+    return spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec
+
+
+@pytest.mark.parametrize("S", [32, 64])
+def test_precision_sweep_by_baseline_decile(oracle_mod, idg, S):
+    spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec = _sample(oracle_mod, S)
+    N, C, rows = md.shape[0], spec.nchannels, obs.uvw.shape[0]
     sp = spec_for(spec.grid_size, S, C, spec.nstations, obs.aterms.shape[0], spec.image_size)
     for variant in (L.VARIANT_PLAIN, L.VARIANT_BATCHED):
         got_g = grid_gpu(sp, md, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, variant, ext=ext)
@@ -84,3 +92,32 @@ def test_precision_sweep_by_baseline_decile(oracle_mod, idg, S):
             assert overall <= TOL, line
             assert max(t["rel_rms"] for t in table) <= TOL, line
         assert np.all(got_v[~covered] == 0)
+
+
+@pytest.mark.parametrize("S", [32, 64])
+def test_channel_recurrence_precision_by_decile(oracle_mod, idg, S):
+    """The batched gridder's channel-recurrence shapes on the precision sweep:
+    64 channels whose float wavenumber steps take three values (chains break
+    where a third one enters and every 16 channels), long baselines whose tiles
+    fall back to per-channel sincos.  Same tolerance, per decile, as the
+    per-channel form (whose error is printed beside it)."""
+    from idg_gb300 import tuning
+
+    spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec = _sample(oracle_mod, S)
+    N, C = md.shape[0], spec.nchannels
+    steps = np.unique(np.diff(obs.wavenumbers))
+    assert steps.size >= 3
+    sp = spec_for(spec.grid_size, S, C, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    ng, _ = tuning.num_shapes()
+    saved = tuning.get_shapes(S)
+    try:
+        for shape in [13] + list(range(15, ng)):
+            tuning.set_shapes(S, shape, saved[1])
+            got_g = grid_gpu(sp, md, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, L.VARIANT_BATCHED, ext=ext)
+            gd = _decile_errors(got_g.reshape(N, -1), want_g.reshape(N, -1), dec)
+            overall = float(np.linalg.norm(got_g - want_g) / np.linalg.norm(want_g))
+            print("[precision] " + json.dumps({"S": S, "gridder_shape": shape, "overall_rel_rms": overall,
+                                               "worst_decile_rel_rms": max(t["rel_rms"] for t in gd)}))
+            assert overall <= TOL and max(t["rel_rms"] for t in gd) <= TOL, (shape, gd)
+    finally:
+        tuning.set_shapes(S, *saved)
