@@ -126,3 +126,44 @@ def test_gridder_degridder_adjoint_fp64(oracle_mod):
     lhs = np.vdot(Gv, P.astype(np.complex128))
     rhs = np.vdot(v.astype(np.complex128), DP)
     assert abs(lhs - rhs) < 1e-9 * abs(lhs)
+
+
+def _point_source(spec, obs, px, py):
+    """Visibilities of a unit point source at the centre of subgrid pixel
+    (px, py): V[t][c][pol] = exp(+i k_c (u l0 + v m0 + w n0)), the same in all
+    four correlations, and the known answer at that pixel of every subgrid:
+    T C exp(i phase_offset(l0, m0)) (identity A-terms, unit taper).  The image
+    size is taken at float32 precision, as the gridders receive it."""
+    S, G, img = spec.subgrid_size, spec.grid_size, float(np.float32(spec.image_size))
+    l0 = (px + 0.5 - S / 2) * img / S
+    m0 = (py + 0.5 - S / 2) * img / S
+    n0 = (l0 * l0 + m0 * m0) / (1.0 + np.sqrt(1.0 - l0 * l0 - m0 * m0))
+    uvw = obs.uvw.astype(np.float64)
+    k = obs.wavenumbers.astype(np.float64)
+    arg = (uvw[:, 0] * l0 + uvw[:, 1] * m0 + uvw[:, 2] * n0)[:, None] * k[None, :]
+    vis = np.repeat(np.exp(1j * arg)[:, :, None], 4, axis=2).astype(np.complex64)
+    md = obs.metadata
+    u_off = (md["x"].astype(np.float64) + S / 2 - G / 2) * 2 * np.pi / img
+    v_off = (md["y"].astype(np.float64) + S / 2 - G / 2) * 2 * np.pi / img
+    want = md["nr_timesteps"] * spec.nchannels * np.exp(1j * (u_off * l0 + v_off * m0))
+    return vis, want
+
+
+def test_point_source_known_answer(oracle_mod):
+    """A point source on a pixel centre grids to T C exp(i phase_offset) at that
+    pixel in every subgrid and correlation, and every other pixel is smaller
+    (FP64 oracle, config-1 geometry, identity A-terms, unit taper)."""
+    import idg_gb300.datasets as D
+
+    spec = D.config1()
+    obs = D.make_observation(spec)
+    S = spec.subgrid_size
+    px, py = S // 2 + 5, S // 2 - 7
+    vis, want = _point_source(spec, obs, px, py)
+    prm = oracle_mod.params(spec.grid_size, S, spec.nchannels, spec.nstations, spec.n_subgrids, spec.image_size)
+    ones = np.ones((S, S), np.float32)
+    got = oracle_mod.gridder(prm, obs.uvw, obs.wavenumbers, vis, ones, obs.aterms, obs.metadata)
+    for pol in range(4):
+        assert np.max(np.abs(got[:, pol, py, px] - want) / np.abs(want)) < 1e-7
+    mag = np.abs(got[:, 0]).reshape(spec.n_subgrids, -1)
+    assert np.all(mag.argmax(axis=1) == py * S + px)
