@@ -68,7 +68,7 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true", help="no CPU baseline (profiling runs)")
     ap.add_argument("--max-subgrids", type=int, default=0, help="use only the first N subgrids of the plan (profiling)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (p50/p99 latency) leg")
-    ap.add_argument("--serve-jobs", type=int, default=10, help="observations in the serving leg (2 jobs each)")
+    ap.add_argument("--serve-jobs", type=int, default=30, help="observations in the serving leg (2 jobs each)")
     ap.add_argument("--serve-rate", type=float, default=16.0, help="mean arrival rate of the serving leg, jobs/s")
     ap.add_argument("--shapes", default="", help="G,D: batched gridder/degridder launch shapes instead of autotuning")
     return ap.parse_args()

@@ -53,8 +53,17 @@ def make_observation(rng, max_vis: float):
 
 def run_stream(observations, rate: float, slots: int = 4, budget_gb: float = 96.0, seed: int = 5) -> dict:
     """Serve the gridding and degridding jobs of `observations` as one Poisson
-    stream of mean rate `rate` jobs/s; returns the latency / throughput line."""
+    stream of mean rate `rate` jobs/s; returns the latency / throughput line.
+    One gridding and one degridding job of the first observation run before
+    the stream (into a grid of their own) so that the server's one-time set-up
+    is not timed; the percentiles are over the stream's jobs (linear
+    interpolation between order statistics)."""
     with Server(max_slots=slots, hbm_budget_bytes=int(budget_gb * (1 << 30)), cta_share=True) as srv:
+        spec0, gjob0, djob0 = observations[0]
+        warm = srv.grid_create(spec0.grid_size)
+        srv.wait(srv.submit(_lib.IDG_JOB_GRID, gjob0, warm))
+        srv.wait(srv.submit(_lib.IDG_JOB_DEGRID, djob0, warm))
+        srv.grid_release(warm)
         grids = [srv.grid_create(spec.grid_size) for spec, _, _ in observations]
         # a random interleaving in which each observation's gridding job precedes its degridding job
         order = np.random.default_rng(seed + 1).permutation(2 * len(observations)).reshape(-1, 2)
@@ -67,21 +76,23 @@ def run_stream(observations, rate: float, slots: int = 4, budget_gb: float = 96.
         for g in grids:
             srv.grid_release(g)
     lat = sorted(j["latency_ms"] for j in st["jobs"])
+    nvis = int(sum(j["visibilities"] for j in st["jobs"]))
     return {
         "metric": "serving: job latency and throughput, Poisson arrivals",
         "rate_jobs_per_s": rate,
         "jobs": len(stream),
-        "completed": st["completed"],
+        "completed": st["completed"] - 2,
         "rejected": st["rejected"],
-        "p50_ms": st["p50_ms"],
-        "p99_ms": st["p99_ms"],
-        "mean_ms": st["mean_ms"],
+        "p50_ms": float(np.percentile(lat, 50)) if lat else None,
+        "p99_ms": float(np.percentile(lat, 99)) if lat else None,
+        "mean_ms": float(np.mean(lat)) if lat else None,
         "max_ms": lat[-1] if lat else None,
-        "mvis_per_s": st["mvis_per_s"],
+        "mvis_per_s": nvis / st["wall_s"] / 1e6,
+        "warmup_jobs": 2,
         "hbm_peak_gb": st["hbm_peak"] / 1e9,
         "slots": slots,
         "budget_gb": budget_gb,
-        "visibilities": int(sum(j["visibilities"] for j in st["jobs"])),
+        "visibilities": nvis,
         "wall_s": st["wall_s"],
     }
 
