@@ -19,7 +19,7 @@
 //    When a tile's bound pi + max|kappa| max|Q| stays below kFastBound the
 //    sincos takes x directly (the SFU reduces the argument itself; the error
 //    grows as |x| * 2^-24), otherwise x is reduced to [-pi, pi] first.
-//  * Shapes 15 and 16 replace the per-channel sincos of those tiles by an
+//  * Shapes 15-17 replace the per-channel sincos of those tiles by an
 //    exact channel recurrence (grid_tile_recur): the autotuner keeps them
 //    when they are faster on the data at hand.
 #include "idg_device.cuh"
@@ -576,6 +576,7 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 //  14: shape 7 with the channel loop unrolled by four
 //  15: 128 x 4, 2 CTAs/SM, Gauss MACs, channel recurrence (chains <= 16), unrolled by four
 //  16: shape 15 with each channel's next phasor computed ahead of its MACs
+//  17: 128 x 3 (whole passes for S = 48), 2 CTAs/SM, Gauss MACs, channel recurrence, unrolled by four
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -597,7 +598,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return 17; }
+int gridder_fast_shapes() { return 18; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -617,6 +618,7 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 14: return launch_shape<128, 4, 256, 2, kGauss | kUnroll4>(a, stream);
     case 15: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kUnroll4>(a, stream);
     case 16: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kPipe | kUnroll4>(a, stream);
+    case 17: return launch_shape<128, 3, 256, 2, kGauss | kRecur | kUnroll4>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }

@@ -43,6 +43,7 @@ def main(argv=None):
     G = parts[0].spec.grid_size
     stream = torch.cuda.Stream(dev)
     groups = []
+    tuned = {}
     nvis = 0
     with torch.cuda.stream(stream):
         grid_p = torch.zeros((1, 4, G, G), dtype=torch.complex64, device=dev)
@@ -63,8 +64,10 @@ def main(argv=None):
             # autotune this size's batched shapes on a leading sample
             ns = min(N, 4096)
             r1 = int(o.metadata["time_offset"][ns - 1] + o.metadata["nr_timesteps"][ns - 1])
-            tuning.autotune(sp, d["md"][:ns], d["uvw"][:r1], d["k"], d["vis"][:r1], d["taper"], d["at"],
-                            d["sub"][:ns], d["vout_b"][:r1], ext=d["ext"][:ns], repeats=1, stream=stream, store=False)
+            res = tuning.autotune(sp, d["md"][:ns], d["uvw"][:r1], d["k"], d["vis"][:r1], d["taper"], d["at"],
+                                  d["sub"][:ns], d["vout_b"][:r1], ext=d["ext"][:ns], repeats=1, stream=stream,
+                                  store=False)
+            tuned[S] = {"gridder": res["gridder"], "degridder": res["degridder"]}
             plan = ops.Plan(sp, o.metadata, rows, ext=o.ext, variant=_lib.VARIANT_BATCHED)
             groups.append((sp, d, plan))
     stream.synchronize()
@@ -112,6 +115,7 @@ def main(argv=None):
         "ratio": ms_p / ms_b,
         "grid_rel_diff": rel(grid_b, grid_p),
         "vis_rel_diff": max(rel(d["vout_b"], d["vout_p"]) for _, d, _ in groups),
+        "tuned_shapes": tuned,
         "steps": args.steps,
         "warmup": args.warmup,
     }
