@@ -49,9 +49,10 @@ METRIC = "Mvis/s grid+degrid vs plain GPU form at ≤1e-5 rel err; p50/p99 job l
 FLOP_PER_PIXVIS = 34.0  # 16 FMA of the four complex MACs + 1 FMA of the phase
 # DRAM bytes (read + write) per subgrid of one batched kernel launch, S = 32, 16
 # channels x 128 timesteps: ncu capture of one launch on the first 8192
-# subgrids of the config-2 plan with the tuned shapes (gridder 686.6 MB read +
-# 244.7 MB written; degridder 419.7 MB read + 490.9 MB written), divided by 8192.
-DRAM_BYTES_PER_SUBGRID = {"gridder": 113682.0, "degridder": 111153.0}
+# subgrids of the config-2 plan with the tuned mirror-quad shapes (gridder
+# 691.7 MB read + 243.1 MB written; degridder 418.3 MB read + 495.2 MB written),
+# divided by 8192.
+DRAM_BYTES_PER_SUBGRID = {"gridder": 114107.0, "degridder": 111513.0}
 
 
 def parse():
@@ -427,7 +428,10 @@ def run_ours(args, rank, world, local_rank):
         e2e = {"value": world * nvis / (e2e_ms * 1e-3) / 1e6, "unit": "Mvis/s",
                "h2d_bytes_per_step": int(totals[-1]["h2d_bytes"]), "d2h_bytes_per_step": int(totals[-1]["d2h_bytes"]),
                "ms_per_step": e2e_ms, "api": "idg_imaging_cycle (C ABI), pinned host buffers",
-               "chunks": (N + chunk - 1) // chunk}
+               "chunks": (N + chunk - 1) // chunk,
+               "gridding_ms": float(np.mean([t["gridding_ms"] for t in totals])),
+               "degridding_ms": float(np.mean([t["degridding_ms"] for t in totals])),
+               "steps_ms": [round(float(t["total_ms"]), 1) for t in totals]}
         # cross-check: the host cycle reproduces the device-resident step's visibilities
         ops.release_buffers()
         del out_host

@@ -69,6 +69,8 @@ __device__ __forceinline__ f2 reduce_2pi(f2 x) {
     return ffma2(k, pack2(-k2PiLo, -k2PiLo), x);
 }
 
+__device__ __forceinline__ f2 neg2(f2 v) { return v ^ 0x8000000080000000ull; }
+
 __device__ __forceinline__ void sincos_pair(f2 x, f2 &c, f2 &s) {
     float x0, x1, s0, c0, s1, c1;
     unpack2(x, x0, x1);
@@ -334,9 +336,294 @@ cudaError_t launch_cp(const KernelArgs &a, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Mirror-quad form of the degridder (shapes 13-15 of this family).  A quad is
+// the four pixels (hx, hy), (-hx, -hy), (-hx, hy), (hx, -hy) of one n; with the
+// gridder's factors P = e^{i a_c hx}, Q = e^{i b_c hy}, R = e^{i g_c n},
+// X = P Q and Y = conj(P) Q, the four pixels' phasors are conj of X R,
+// conj(X) R, Y R and conj(Y) R, so the quad contributes
+//   V += conj(R) Z,  Z = P00 conj(X) + P11 X + P10 conj(Y) + P01 Y
+// (P00 = pixel (hx, hy), P11 = (-hx, -hy), P10 = (-hx, hy), P01 = (hx, -hy)).
+// With the quad's sums and differences staged once (per correlation
+// s = P00 + P11, d = (P11.re - P00.re, P00.im - P11.im) and the same for the
+// Y pair), Z costs 8 FMA per correlation and conj(R) Z 4: 3 per pixel and
+// correlation against the Gauss form's 3 plus a sincos per pixel, with three
+// sincos per quad (1.5 SFU operations per pixel-visibility instead of 2).
+// Work split as the channel-pair kernel: a group is one timestep x CB channels,
+// its four lanes split the staged quads, channels sit in the packed halves.
+// ---------------------------------------------------------------------------
+struct QuadLayout {
+    size_t ops, geo, coef, kappa, total;
+};
+// 256 B of operands per quad padded to 272 B, so that the four lanes of a
+// group (consecutive quads) read distinct banks: 68 words apart = 4 banks apart.
+constexpr uint32_t kQuadStride = 272;
+
+__host__ __device__ inline QuadLayout quad_layout(int S, int C, int batch) {
+    QuadLayout L;
+    size_t off = 64;
+    L.ops = off;   off += (size_t)batch * kQuadStride;    // 32 packed operands per quad, padded
+    L.geo = off;   off += (size_t)batch * 16;             // (hx, hy, n, 0) of the quad's (hx, hy) pixel
+    L.coef = off;  off += (size_t)kTimeTile * 32;         // (a, b, g, qu) (qv, qw, -, -) per timestep
+    L.kappa = off; off += (size_t)(C + kMaxCB) * 4;       // kappa per channel, zero padded
+    L.total = (off + 15) & ~size_t(15);
+    return L;
+}
+
+template <int NPAIR, bool FAST>
+__device__ __forceinline__ void quad_macs(f2 (&acc)[NPAIR][4][2], const f2 (&kp)[NPAIR], float4 g, float A, float B,
+                                          float Gc, float qu, float qv, float qw, uint32_t ops_addr) {
+    const float tx = reduce_2pi_s(A * g.x), ty = reduce_2pi_s(B * g.y), tn = reduce_2pi_s(Gc * g.z);
+    const f2 TX = pack2(tx, tx), TY = pack2(ty, ty), TN = pack2(tn, tn);
+    const float qx = qu * g.x, qy = qv * g.y, qn = qw * g.z;
+    const f2 QX = pack2(qx, qx), QY = pack2(qy, qy), QN = pack2(qn, qn);
+    // per correlation k: o[8k..8k+7] = (s_r, d_i, s'_r, d'_i, s_i, d_r, s'_i, d'_r), each duplicated
+    f2 o[32];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) lds2(ops_addr + 16 * q, o[2 * q], o[2 * q + 1]);
+#pragma unroll
+    for (int j = 0; j < NPAIR; ++j) {
+        f2 ap = ffma2(kp[j], QX, TX), aq = ffma2(kp[j], QY, TY), ar = ffma2(kp[j], QN, TN);
+        if (!FAST) {
+            ap = reduce_2pi(ap);
+            aq = reduce_2pi(aq);
+            ar = reduce_2pi(ar);
+        }
+        f2 Pc, Ps, Qc, Qs, Rc, Rs;
+        sincos_pair(ap, Pc, Ps);
+        sincos_pair(aq, Qc, Qs);
+        sincos_pair(ar, Rc, Rs);
+        const f2 nPs = neg2(Ps), nRs = neg2(Rs);
+        const f2 m1 = fmul2(Pc, Qc), m3 = fmul2(Pc, Qs);
+        const f2 Xr = ffma2(nPs, Qs, m1), Yr = ffma2(Ps, Qs, m1);
+        const f2 Xi = ffma2(Ps, Qc, m3), Yi = ffma2(nPs, Qc, m3);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const f2 *p = o + 8 * k;
+            const f2 Zr = ffma2(Yi, p[3], ffma2(Yr, p[2], ffma2(Xi, p[1], fmul2(Xr, p[0]))));
+            const f2 Zi = ffma2(Yi, p[7], ffma2(Yr, p[6], ffma2(Xi, p[5], fmul2(Xr, p[4]))));
+            // V += conj(R) Z
+            acc[j][k][0] = ffma2(Rs, Zi, ffma2(Rc, Zr, acc[j][k][0]));
+            acc[j][k][1] = ffma2(nRs, Zr, ffma2(Rc, Zi, acc[j][k][1]));
+        }
+    }
+}
+
+template <int NT, int QB, int MINB, int CB, int UNR>
+__global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) {
+    constexpr int kT = NT, kCB = CB, kNP = CB / 2;
+    static_assert(CB == 4 || CB == 8, "channel groups of 4 or 8");
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int S = a.S, S2 = S * S, Sh = S / 2, nquads = Sh * Sh;
+    const QuadLayout L = quad_layout(S, a.C, QB);
+    Head *head = reinterpret_cast<Head *>(smem);
+    float4 *ops = reinterpret_cast<float4 *>(smem + L.ops);
+    float4 *geo = reinterpret_cast<float4 *>(smem + L.geo);
+    float4 *coef = reinterpret_cast<float4 *>(smem + L.coef);
+    float *kap = reinterpret_cast<float *>(smem + L.kappa);
+    const uint32_t ops_addr = smem_addr(ops);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gw = lane / kLanes, part = lane % kLanes;
+    const bool refcpu = (a.flags & IDG_FLAG_DEGRID_ATERM_REFCPU) != 0;
+    const bool taper = (a.flags & IDG_FLAG_NO_TAPER) == 0;
+    const double d2pi = (double)a.image_size / (double)S / kTwoPi;
+    const float hmax = 0.5f * (float)(S - 1);
+    const float nmax = pixel_geometry(0, S, a.image_size).z;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            head->next = atomicAdd(a.work_counter, 1);
+            head->kmax_bits = 0;
+            head->qmax_bits = 0;
+        }
+        __syncthreads();
+        const int idx = head->next;
+        if (idx >= a.nr_subgrids) break;
+        const int s = a.work_list ? a.work_list[idx] : idx;
+        const SubgridInfo si = load_subgrid(a, s);
+        if (!si.ok) {
+            if (tid == 0) flag_status(a.status, kStatusBadPlan);
+            continue;
+        }
+        const int nc = si.c1 - si.c0;
+        const int ncb = (nc + kCB - 1) / kCB;
+        const int cref = si.c0 + (nc > 0 ? (nc - 1) / 2 : 0);
+        const double kref = nc > 0 ? (double)a.wavenumbers[cref] : 0.0;
+        float kmax = 0.f;
+        for (int c = tid; c < ncb * kCB; c += kT) {
+            float kv = 0.f;
+            if (c < nc) kv = (float)((double)a.wavenumbers[si.c0 + c] - kref);
+            kap[c] = kv;
+            kmax = fmaxf(kmax, fabsf(kv));
+        }
+        if (kmax > 0.f) atomicMax(&head->kmax_bits, __float_as_int(kmax));
+        const size_t jones_stride = (size_t)S2 * 2;
+        const float4 *a1 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st1) * jones_stride;
+        const float4 *a2 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st2) * jones_stride;
+
+        for (int qb = 0; qb < nquads; qb += QB) {
+            const int nq = min(QB, nquads - qb);
+            __syncthreads(); // previous batch consumed
+            // ---- stage the batch's quads: A-terms and taper applied, sums and differences
+            for (int i = tid; i < nq; i += kT) {
+                const int g = qb + i, gy = g / Sh, gx = g - gy * Sh;
+                // 0 = (gx, gy), 1 = (S-1-gx, S-1-gy), 2 = (S-1-gx, gy), 3 = (gx, S-1-gy)
+                const int qx[4] = {gx, S - 1 - gx, S - 1 - gx, gx};
+                const int qy[4] = {gy, S - 1 - gy, gy, S - 1 - gy};
+                cf v[4][4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int q = qy[e] * S + qx[e];
+                    const float sph = taper ? a.taper[q] : 1.f;
+#pragma unroll
+                    for (int pol = 0; pol < 4; ++pol) {
+                        const float2 x = a.subgrids[((size_t)s * 4 + pol) * S2 + q];
+                        v[e][pol] = {sph * x.x, sph * x.y};
+                    }
+                    cf j1[4], j2[4];
+                    load_jones(a1 + 2 * q, j1);
+                    load_jones(a2 + 2 * q, j2);
+                    if (refcpu)
+                        aterm_gridder(v[e], j1, j2);
+                    else
+                        aterm_adjoint(v[e], j1, j2);
+                }
+                float4 *d = ops + (kQuadStride / 16) * i;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const cf p00 = v[0][k], p11 = v[1][k], p10 = v[2][k], p01 = v[3][k];
+                    const float e8[8] = {p00.re + p11.re, p00.im - p11.im, p10.re + p01.re, p10.im - p01.im,
+                                         p00.im + p11.im, p11.re - p00.re, p10.im + p01.im, p01.re - p10.re};
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+                        d[4 * k + r] = make_float4(e8[2 * r], e8[2 * r], e8[2 * r + 1], e8[2 * r + 1]);
+                }
+                const float3 gg = pixel_geometry(gy * S + gx, S, a.image_size);
+                geo[i] = make_float4(gg.x, gg.y, gg.z, 0.f);
+            }
+
+            for (int t0 = 0; t0 < si.T; t0 += kTimeTile) {
+                const int tt = min(kTimeTile, si.T - t0);
+                __syncthreads();
+                for (int t = tid; t < tt; t += kT) {
+                    const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
+                    const double u = p[0], v = p[1], w = p[2];
+                    double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
+                    double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
+                    ca -= 2.0 * rint(ca * 0.5);
+                    cbv -= 2.0 * rint(cbv * 0.5);
+                    const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
+                    const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
+                    coef[2 * t + 0] = make_float4((float)(kTwoPi * ca), (float)(kTwoPi * cbv), (float)cg, qu);
+                    coef[2 * t + 1] = make_float4(qv, qw, 0.f, 0.f);
+                    const float qm = fmaxf(fmaxf(fabsf(qu) * hmax, fabsf(qv) * hmax), fabsf(qw) * nmax);
+                    atomicMax(&head->qmax_bits, __float_as_int(qm));
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    head->fast = (3.1416f + __int_as_float(head->kmax_bits) * __int_as_float(head->qmax_bits)) <= kFastBound;
+                    head->qmax_bits = 0;
+                }
+                __syncthreads();
+                const bool fast = head->fast != 0;
+                const int ngroups = tt * ncb;
+                for (int gbase = warp * kGroupsPerWarp; gbase < ngroups; gbase += (kT / 32) * kGroupsPerWarp) {
+                    const int grp = gbase + gw;
+                    const bool active = grp < ngroups;
+                    const int gg = active ? grp : 0;
+                    const int t = gg / ncb, cfirst = (gg - t * ncb) * kCB;
+                    const float4 c0 = coef[2 * t], c1 = coef[2 * t + 1];
+                    f2 kp[kNP];
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j) kp[j] = pack2(kap[cfirst + 2 * j], kap[cfirst + 2 * j + 1]);
+                    f2 acc[kNP][4][2];
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j)
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) acc[j][k][0] = acc[j][k][1] = 0ull;
+                    if (fast) {
+#pragma unroll UNR
+                        for (int i = part; i < nq; i += kLanes)
+                            quad_macs<kNP, true>(acc, kp, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                 ops_addr + kQuadStride * (uint32_t)i);
+                    } else {
+#pragma unroll UNR
+                        for (int i = part; i < nq; i += kLanes)
+                            quad_macs<kNP, false>(acc, kp, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                  ops_addr + kQuadStride * (uint32_t)i);
+                    }
+                    // combine the four lanes
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j)
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+#pragma unroll
+                            for (int r = 0; r < 2; ++r) {
+                                f2 v = acc[j][k][r];
+                                v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 1));
+                                v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 2));
+                                acc[j][k][r] = v;
+                            }
+                    if (active) {
+                        float4 *row = a.vis + ((int64_t)si.row0 + t0 + t) * a.C * 2;
+#pragma unroll
+                        for (int j = 0; j < kNP; ++j) {
+                            if (j % kLanes != part) continue;
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                if (cfirst + 2 * j + h >= nc) continue;
+                                const int c = si.c0 + cfirst + 2 * j + h;
+                                float w[8];
+#pragma unroll
+                                for (int k = 0; k < 4; ++k)
+#pragma unroll
+                                    for (int r = 0; r < 2; ++r) {
+                                        float lo, hi;
+                                        unpack2(acc[j][k][r], lo, hi);
+                                        w[2 * k + r] = h ? hi : lo;
+                                    }
+                                float4 va = make_float4(w[0], w[1], w[2], w[3]);
+                                float4 vb = make_float4(w[4], w[5], w[6], w[7]);
+                                if (qb > 0) {
+                                    const float4 oa = row[2 * c], ob = row[2 * c + 1];
+                                    va = make_float4(va.x + oa.x, va.y + oa.y, va.z + oa.z, va.w + oa.w);
+                                    vb = make_float4(vb.x + ob.x, vb.y + ob.y, vb.z + ob.z, vb.w + ob.w);
+                                }
+                                row[2 * c] = va;
+                                row[2 * c + 1] = vb;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int NT, int QB, int MINB, int CB, int UNR>
+cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
+    if (a.S % 2 != 0) return cudaErrorInvalidValue;
+    auto kern = degridder_quad_kernel<NT, QB, MINB, CB, UNR>;
+    const size_t smem = quad_layout(a.S, a.C, QB).total;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (a.max_ctas > 0 && blocks > a.max_ctas) blocks = a.max_ctas;
+    if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
+    kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
 } // namespace
 
-int degridder_cp_shapes() { return 13; }
+int degridder_cp_shapes() { return 16; }
 
 // Channel-pair shapes (index within this family):
 //   0: 128 threads, 8-channel groups, 256-pixel batches, 4 CTAs/SM (16 warps)
@@ -352,8 +639,14 @@ int degridder_cp_shapes() { return 13; }
 //  10: shape 7 with 256-pixel batches
 //  11: shape 8 with the pixel loop unrolled by four
 //  12: shape 6 with the pixel loop unrolled by eight
+//  13: mirror quads, 128 threads, 8-channel groups, 256-quad batches, 2 CTAs/SM
+//  14: mirror quads, 128 threads, 8-channel groups, 256-quad batches, 3 CTAs/SM (12 warps)
+//  15: shape 13 with the quad loop unrolled by two
 cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
+    case 13: return launch_quad<128, 256, 2, 8, 1>(a, stream);
+    case 14: return launch_quad<128, 256, 3, 8, 1>(a, stream);
+    case 15: return launch_quad<128, 256, 2, 8, 2>(a, stream);
     case 1: return launch_cp<128, 512, 3, 8, 0, 2>(a, stream);
     case 2: return launch_cp<128, 512, 2, 16, 0, 1>(a, stream);
     case 3: return launch_cp<128, 512, 3, 8, kGaussCp, 1>(a, stream);

@@ -558,6 +558,320 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mirror-quad form (shapes 18-21).  The pixels of a subgrid come in quads
+// (hx, hy), (-hx, hy), (hx, -hy), (-hx, -hy) (pixel x and S-1-x have opposite
+// hx exactly, and all four share n).  The phase of channel c is
+//   x_c = a_c hx + b_c hy + g_c n,  a_c = A + kappa_c qu, b_c = B + kappa_c qv,
+//   g_c = G + kappa_c qw
+// (the same per-timestep coefficients as above, regrouped by pixel factor), so
+// with P = e^{i a_c hx}, Q = e^{i b_c hy}, R = e^{i g_c n}, X = P Q, Y = conj(P) Q
+// and W = V R the four pixels receive W X, W conj(X), W Y, W conj(Y).  W X and
+// W conj(X) share their four real products (Wr Xr, Wi Xi, Wr Xi, Wi Xr): summed
+// separately over all visibilities they give both pixels in the epilogue, so a
+// quad costs 8 FMA per correlation per visibility (2 per pixel, against 3 for
+// the Gauss form), plus W = V R (4 per correlation, shared by the quad) and
+// X, Y (6).  Per pixel-visibility: 14.25 FMA and 1.5 SFU operations (three
+// sincos per quad), against 14 FMA and 2 SFU operations per pixel above, and
+// 8 accumulators per pixel instead of 12.
+// Each thread owns GP pairs of quads; the two quads of a pair sit in the two
+// halves of the packed FP32x2 registers.  Per (timestep, quad pair) the
+// factors' offsets tau = A hx, B hy, G n are reduced to [-pi, pi] once; per
+// channel the arguments are tau + kappa_c (qu hx, qv hy, qw n), below the
+// unreduced-sincos bound on fast tiles and reduced otherwise.
+// ---------------------------------------------------------------------------
+// SHP: every quad of the thread has the same x column (NT a multiple of S/2),
+// so P is one sincos per thread, shared by all its quads.
+template <int GP, bool FAST, int UNR, bool SHP>
+__device__ __forceinline__ void quad_tile(f2 (&acc)[GP][4][8], const f2 (&hx)[GP], const f2 (&hy)[GP],
+                                          const f2 (&nn)[GP], const float4 *coef, const float4 *vq, const f2 *kp,
+                                          int tt, int ncc) {
+    for (int t = 0; t < tt; ++t) {
+        const float4 c0 = coef[3 * t], c1 = coef[3 * t + 1], c2 = coef[3 * t + 2];
+        const f2 A2 = pack2(c0.x, c0.y), B2 = pack2(c0.z, c0.w), G2 = pack2(c1.x, c1.y);
+        const f2 QU = pack2(c1.z, c1.w), QV = pack2(c2.x, c2.y), QW = pack2(c2.z, c2.w);
+        f2 tx[GP], ty[GP], tn[GP], qx[GP], qy[GP], qn[GP];
+#pragma unroll
+        for (int j = 0; j < GP; ++j) {
+            tx[j] = reduce_2pi(fmul2(A2, hx[j]));
+            ty[j] = reduce_2pi(fmul2(B2, hy[j]));
+            tn[j] = reduce_2pi(fmul2(G2, nn[j]));
+            qx[j] = fmul2(QU, hx[j]);
+            qy[j] = fmul2(QV, hy[j]);
+            qn[j] = fmul2(QW, nn[j]);
+        }
+        const float4 *vt = vq + (size_t)t * ncc * 4;
+#pragma unroll UNR
+        for (int c = 0; c < ncc; ++c) {
+            const f2 kc = kp[c];
+            // visibility operands, duplicated into both halves: (vr, vr), (vi, vi) per correlation
+            f2 vr[4], vi[4];
+            const uint32_t base = smem_addr(vt + 4 * c);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) lds2(base + 16 * k, vr[k], vi[k]);
+            f2 Pc0 = 0ull, Ps0 = 0ull;
+            if (SHP) {
+                f2 ap = ffma2(kc, qx[0], tx[0]);
+                if (!FAST) ap = reduce_2pi(ap);
+                float a0, a1, sn, cs;
+                unpack2(ap, a0, a1);
+                __sincosf(a0, &sn, &cs);
+                Pc0 = dup(cs);
+                Ps0 = dup(sn);
+            }
+#pragma unroll
+            for (int j = 0; j < GP; ++j) {
+                f2 aq = ffma2(kc, qy[j], ty[j]), ar = ffma2(kc, qn[j], tn[j]);
+                if (!FAST) {
+                    aq = reduce_2pi(aq);
+                    ar = reduce_2pi(ar);
+                }
+                f2 Pc = Pc0, Ps = Ps0, Qc, Qs, Rc, Rs;
+                if (!SHP) {
+                    f2 ap = ffma2(kc, qx[j], tx[j]);
+                    if (!FAST) ap = reduce_2pi(ap);
+                    sincos_pair<false>(ap, Pc, Ps);
+                }
+                sincos_pair<false>(aq, Qc, Qs);
+                sincos_pair<false>(ar, Rc, Rs);
+                // X = P Q, Y = conj(P) Q
+                const f2 nPs = neg2(Ps);
+                const f2 m1 = fmul2(Pc, Qc), m3 = fmul2(Pc, Qs);
+                const f2 Xr = ffma2(nPs, Qs, m1), Yr = ffma2(Ps, Qs, m1);
+                const f2 Xi = ffma2(Ps, Qc, m3), Yi = ffma2(nPs, Qc, m3);
+                const f2 nRs = neg2(Rs);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    // W = V R
+                    const f2 Wr = ffma2(vr[k], Rc, fmul2(vi[k], nRs));
+                    const f2 Wi = ffma2(vr[k], Rs, fmul2(vi[k], Rc));
+                    f2 *q = acc[j][k];
+                    q[0] = ffma2(Wr, Xr, q[0]);
+                    q[1] = ffma2(Wi, Xi, q[1]);
+                    q[2] = ffma2(Wr, Xi, q[2]);
+                    q[3] = ffma2(Wi, Xr, q[3]);
+                    q[4] = ffma2(Wr, Yr, q[4]);
+                    q[5] = ffma2(Wi, Yi, q[5]);
+                    q[6] = ffma2(Wr, Yi, q[6]);
+                    q[7] = ffma2(Wi, Yr, q[7]);
+                }
+            }
+        }
+    }
+}
+
+// Kernel of the mirror-quad form: NT threads, GP quad pairs per thread per
+// pass, TV visibilities per staged tile, at least MINB CTAs per SM.  Staging,
+// coefficients, work distribution and failure handling as gridder_fast_kernel.
+template <int NT, int GP, int TV, int MINB, int UNR>
+__global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
+    constexpr int kT = NT, kPassQuads = NT * GP * 2, kTileVis = TV, kMaxChunk = TV;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int S = a.S, S2 = S * S, Sh = S / 2, nquads = Sh * Sh;
+    // quad g of a pass has x column g mod Sh; with NT a multiple of Sh every quad
+    // of a thread (offsets multiples of NT) is in the thread's column
+    const bool shared_x = NT % Sh == 0;
+    const Layout L = layout(S, a.C, TV);
+    SmemHead *head = reinterpret_cast<SmemHead *>(smem);
+    float4 *raw = reinterpret_cast<float4 *>(smem + L.raw);
+    float4 *vq = reinterpret_cast<float4 *>(smem + L.vexp);
+    float4 *coef = reinterpret_cast<float4 *>(smem + L.coef);
+    f2 *kap = reinterpret_cast<f2 *>(smem + L.kappa);
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        mbar_init(&head->bar, 1);
+        mbar_init_fence();
+        head->abort = 0;
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const double d2pi = (double)a.image_size / (double)S / kTwoPi;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            head->next = atomicAdd(a.work_counter, 1);
+            head->kmax_bits = 0;
+            head->qmax_bits = 0;
+        }
+        __syncthreads();
+        const int idx = head->next;
+        if (idx >= a.nr_subgrids || head->abort) break;
+        const int s = a.work_list ? a.work_list[idx] : idx;
+        const SubgridInfo si = load_subgrid(a, s);
+        const int nc = si.c1 - si.c0;
+        if (!si.ok) {
+            if (tid == 0) flag_status(a.status, kStatusBadPlan);
+            for (int i = tid; i < 4 * S2; i += kT) a.subgrids[(size_t)s * 4 * S2 + i] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const int cref = si.c0 + (nc > 0 ? (nc - 1) / 2 : 0);
+        const double kref = nc > 0 ? (double)a.wavenumbers[cref] : 0.0;
+        float kmax = 0.f;
+        for (int c = tid; c < nc; c += kT) {
+            const float kv = (float)((double)a.wavenumbers[si.c0 + c] - kref);
+            kap[c] = dup(kv);
+            kmax = fmaxf(kmax, fabsf(kv));
+        }
+        if (kmax > 0.f) atomicMax(&head->kmax_bits, __float_as_int(kmax));
+        __syncthreads();
+        const float kappa_max = __int_as_float(head->kmax_bits);
+
+        const int chunk = nc < kMaxChunk ? nc : kMaxChunk;
+        const int TT = nc > 0 ? min(kMaxTT, kTileVis / chunk) : 1;
+        const float hmax = 0.5f * (float)(S - 1);
+        const float nmax = pixel_geometry(0, S, a.image_size).z;
+
+        for (int pass = 0; pass * kPassQuads < nquads; ++pass) {
+            f2 acc[GP][4][8];
+#pragma unroll
+            for (int j = 0; j < GP; ++j)
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) acc[j][k][r] = 0ull;
+            // the quads of this thread: pair j holds quads g0 (low half) and g1 (high half);
+            // each quad is named by its pixel (gx, gy) in the low-x, low-y quadrant
+            int qd[GP][2];
+            f2 hx[GP], hy[GP], nn[GP];
+#pragma unroll
+            for (int j = 0; j < GP; ++j) {
+                float gxh[2], gyh[2], gnn[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int g = pass * kPassQuads + (2 * j + h) * kT + tid;
+                    qd[j][h] = g < nquads ? g : -1;
+                    const int gg = g < nquads ? g : 0;
+                    const int gy = gg / Sh, gx = gg - gy * Sh;
+                    const float3 geo = pixel_geometry(gy * S + gx, S, a.image_size);
+                    gxh[h] = geo.x;
+                    gyh[h] = geo.y;
+                    gnn[h] = geo.z;
+                }
+                hx[j] = pack2(gxh[0], gxh[1]);
+                hy[j] = pack2(gyh[0], gyh[1]);
+                nn[j] = pack2(gnn[0], gnn[1]);
+            }
+
+            for (int cb = 0; cb < nc; cb += chunk) {
+                const int ncc = min(chunk, nc - cb);
+                for (int t0 = 0; t0 < si.T; t0 += TT) {
+                    const int tt = min(TT, si.T - t0);
+                    __syncthreads(); // previous tile fully consumed (raw, vq, coef)
+                    if (tid == 0) {
+                        const uint32_t row_bytes = (uint32_t)ncc * 32u;
+                        fence_proxy_async();
+                        mbar_arrive_expect_tx(&head->bar, row_bytes * (uint32_t)tt);
+                        const float4 *src = a.vis + ((int64_t)si.row0 + t0) * a.C * 2 + (int64_t)(si.c0 + cb) * 2;
+                        for (int r = 0; r < tt; ++r)
+                            bulk_g2s(raw + (size_t)r * ncc * 2, src + (int64_t)r * a.C * 2, row_bytes, &head->bar);
+                    }
+                    for (int t = tid; t < tt; t += kT) {
+                        const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
+                        const double u = p[0], v = p[1], w = p[2];
+                        double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
+                        double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
+                        ca -= 2.0 * rint(ca * 0.5);
+                        cbv -= 2.0 * rint(cbv * 0.5);
+                        const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
+                        const float A = (float)(kTwoPi * ca), B = (float)(kTwoPi * cbv), Gv = (float)cg;
+                        const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
+                        coef[3 * t + 0] = make_float4(A, A, B, B);
+                        coef[3 * t + 1] = make_float4(Gv, Gv, qu, qu);
+                        coef[3 * t + 2] = make_float4(qv, qv, qw, qw);
+                        const float qm = fmaxf(fmaxf(fabsf(qu) * hmax, fabsf(qv) * hmax), fabsf(qw) * nmax);
+                        atomicMax(&head->qmax_bits, __float_as_int(qm));
+                    }
+                    if (!mbar_wait_bounded(&head->bar, phase, kWaitNs)) {
+                        head->abort = 1;
+                        flag_status(a.status, kStatusTimeout);
+                    }
+                    __syncthreads();
+                    if (head->abort) {
+                        if (tid == 0) mbar_wait_bounded(&head->bar, phase, kWaitNs);
+                        break;
+                    }
+                    phase ^= 1u;
+                    // expand: per visibility and correlation (re, re, im, im)
+                    for (int i = tid; i < tt * ncc; i += kT) {
+                        const float4 v0 = raw[2 * i], v1 = raw[2 * i + 1];
+                        float4 *d = vq + 4 * i;
+                        d[0] = make_float4(v0.x, v0.x, v0.y, v0.y);
+                        d[1] = make_float4(v0.z, v0.z, v0.w, v0.w);
+                        d[2] = make_float4(v1.x, v1.x, v1.y, v1.y);
+                        d[3] = make_float4(v1.z, v1.z, v1.w, v1.w);
+                    }
+                    if (tid == 0) {
+                        // each factor's argument stays within pi + max|kappa| max|q h|
+                        head->fast = (3.1416f + kappa_max * __int_as_float(head->qmax_bits)) <= kFastBound ? 1 : 0;
+                        head->qmax_bits = 0;
+                    }
+                    __syncthreads();
+                    if (shared_x) {
+                        if (head->fast)
+                            quad_tile<GP, true, UNR, true>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                        else
+                            quad_tile<GP, false, UNR, true>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                    } else if (head->fast) {
+                        quad_tile<GP, true, UNR, false>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                    } else {
+                        quad_tile<GP, false, UNR, false>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                    }
+                }
+                if (head->abort) break;
+            }
+            if (head->abort) break;
+
+            // ---- epilogue: the four pixels of each quad, A-terms, taper
+            const size_t jones_stride = (size_t)S2 * 2;
+            const float4 *a1 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st1) * jones_stride;
+            const float4 *a2 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st2) * jones_stride;
+            const bool taper = (a.flags & IDG_FLAG_NO_TAPER) == 0;
+#pragma unroll
+            for (int j = 0; j < GP; ++j) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (qd[j][h] < 0) continue;
+                    const int gy = qd[j][h] / Sh, gx = qd[j][h] - gy * Sh;
+                    // pixels: 0 = (gx, gy) -> W X ; 1 = (S-1-gx, S-1-gy) -> W conj(X)
+                    //         2 = (S-1-gx, gy) -> W Y ; 3 = (gx, S-1-gy) -> W conj(Y)
+                    const int qx[4] = {gx, S - 1 - gx, S - 1 - gx, gx};
+                    const int qy[4] = {gy, S - 1 - gy, gy, S - 1 - gy};
+                    cf px[4][4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        float r[8];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            float lo, hi;
+                            unpack2(acc[j][k][i], lo, hi);
+                            r[i] = h ? hi : lo;
+                        }
+                        px[0][k] = {r[0] - r[1], r[2] + r[3]};
+                        px[1][k] = {r[0] + r[1], r[3] - r[2]};
+                        px[2][k] = {r[4] - r[5], r[6] + r[7]};
+                        px[3][k] = {r[4] + r[5], r[7] - r[6]};
+                    }
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int q = qy[e] * S + qx[e];
+                        cf j1[4], j2[4];
+                        load_jones(a1 + 2 * q, j1);
+                        load_jones(a2 + 2 * q, j2);
+                        aterm_gridder(px[e], j1, j2);
+                        const float sph = taper ? a.taper[q] : 1.f;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            a.subgrids[((size_t)s * 4 + k) * S2 + q] = make_float2(px[e][k].re * sph, px[e][k].im * sph);
+                    }
+                }
+            }
+        }
+        if (head->abort) break;
+    }
+}
+
 // Launch shapes the autotuner chooses from (index = batched-gridder shape id):
 //   0: 128 threads x 4 pairs, 256-visibility tiles, 3 CTAs/SM (12 warps), plain channel loop
 //   1: 128 x 4, 2 CTAs/SM (8 warps), software-pipelined channel loop, registers uncapped
@@ -577,6 +891,10 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 //  15: 128 x 4, 2 CTAs/SM, Gauss MACs, channel recurrence (chains <= 16), unrolled by four
 //  16: shape 15 with each channel's next phasor computed ahead of its MACs
 //  17: 128 x 3 (whole passes for S = 48), 2 CTAs/SM, Gauss MACs, channel recurrence, unrolled by four
+//  18: mirror quads, 128 threads x 2 quads, 3 CTAs/SM (12 warps), channel loop unrolled by four
+//  19: mirror quads, 128 threads x 2 quads, 2 CTAs/SM (8 warps), registers uncapped
+//  20: mirror quads, 64 threads x 4 quads, 4 CTAs/SM (8 warps), unrolled by two (whole passes for S = 32)
+//  21: mirror quads, 128 threads x 4 quads, 2 CTAs/SM (8 warps), unrolled by two (whole passes for S = 64)
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -596,9 +914,29 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+template <int NT, int GP, int TV, int MINB, int UNR>
+cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
+    if (a.S % 2 != 0) return cudaErrorInvalidValue;
+    auto kern = gridder_quad_kernel<NT, GP, TV, MINB, UNR>;
+    const size_t smem = layout(a.S, a.C, TV).total;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (a.max_ctas > 0 && blocks > a.max_ctas) blocks = a.max_ctas;
+    if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
+    kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
 } // namespace
 
-int gridder_fast_shapes() { return 18; }
+int gridder_fast_shapes() { return 22; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -619,6 +957,10 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 15: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kUnroll4>(a, stream);
     case 16: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kPipe | kUnroll4>(a, stream);
     case 17: return launch_shape<128, 3, 256, 2, kGauss | kRecur | kUnroll4>(a, stream);
+    case 18: return launch_quad<128, 1, 256, 3, 4>(a, stream);
+    case 19: return launch_quad<128, 1, 256, 2, 4>(a, stream);
+    case 20: return launch_quad<64, 2, 256, 4, 2>(a, stream);
+    case 21: return launch_quad<128, 2, 256, 2, 2>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }
