@@ -337,7 +337,7 @@ cudaError_t launch_cp(const KernelArgs &a, cudaStream_t stream) {
 }
 
 // ---------------------------------------------------------------------------
-// Mirror-quad form of the degridder (shapes 13-15 of this family).  A quad is
+// Mirror-quad form of the degridder (shapes 13-16 of this family).  A quad is
 // the four pixels (hx, hy), (-hx, -hy), (-hx, hy), (hx, -hy) of one n; with the
 // gridder's factors P = e^{i a_c hx}, Q = e^{i b_c hy}, R = e^{i g_c n},
 // X = P Q and Y = conj(P) Q, the four pixels' phasors are conj of X R,
@@ -370,8 +370,16 @@ __host__ __device__ inline QuadLayout quad_layout(int S, int C, int batch) {
     return L;
 }
 
-template <int NPAIR, bool FAST>
-__device__ __forceinline__ void quad_macs(f2 (&acc)[NPAIR][4][2], const f2 (&kp)[NPAIR], float4 g, float A, float B,
+// KP: the channel pairs' kappa, either f2 registers (f2[NPAIR]) or a pointer
+// to the group's first channel in shared memory (read per channel pair).
+__device__ __forceinline__ f2 kappa_pair(const f2 (&kp)[4], int j) { return kp[j]; }
+__device__ __forceinline__ f2 kappa_pair(const f2 (&kp)[8], int j) { return kp[j]; }
+__device__ __forceinline__ f2 kappa_pair(const float *kp, int j) {
+    return *reinterpret_cast<const f2 *>(kp + 2 * j);
+}
+
+template <int NPAIR, bool FAST, typename KP>
+__device__ __forceinline__ void quad_macs(f2 (&acc)[NPAIR][4][2], const KP &kp, float4 g, float A, float B,
                                           float Gc, float qu, float qv, float qw, uint32_t ops_addr) {
     const float tx = reduce_2pi_s(A * g.x), ty = reduce_2pi_s(B * g.y), tn = reduce_2pi_s(Gc * g.z);
     const f2 TX = pack2(tx, tx), TY = pack2(ty, ty), TN = pack2(tn, tn);
@@ -383,7 +391,8 @@ __device__ __forceinline__ void quad_macs(f2 (&acc)[NPAIR][4][2], const f2 (&kp)
     for (int q = 0; q < 16; ++q) lds2(ops_addr + 16 * q, o[2 * q], o[2 * q + 1]);
 #pragma unroll
     for (int j = 0; j < NPAIR; ++j) {
-        f2 ap = ffma2(kp[j], QX, TX), aq = ffma2(kp[j], QY, TY), ar = ffma2(kp[j], QN, TN);
+        const f2 kj = kappa_pair(kp, j);
+        f2 ap = ffma2(kj, QX, TX), aq = ffma2(kj, QY, TY), ar = ffma2(kj, QN, TN);
         if (!FAST) {
             ap = reduce_2pi(ap);
             aq = reduce_2pi(aq);
@@ -409,7 +418,7 @@ __device__ __forceinline__ void quad_macs(f2 (&acc)[NPAIR][4][2], const f2 (&kp)
     }
 }
 
-template <int NT, int QB, int MINB, int CB, int UNR>
+template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false>
 __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) {
     constexpr int kT = NT, kCB = CB, kNP = CB / 2;
     static_assert(CB == 4 || CB == 8, "channel groups of 4 or 8");
@@ -542,16 +551,27 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
                     for (int j = 0; j < kNP; ++j)
 #pragma unroll
                         for (int k = 0; k < 4; ++k) acc[j][k][0] = acc[j][k][1] = 0ull;
+                    const float *kps = kap + cfirst;
                     if (fast) {
 #pragma unroll UNR
-                        for (int i = part; i < nq; i += kLanes)
-                            quad_macs<kNP, true>(acc, kp, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
-                                                 ops_addr + kQuadStride * (uint32_t)i);
+                        for (int i = part; i < nq; i += kLanes) {
+                            if (KSM)
+                                quad_macs<kNP, true>(acc, kps, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                     ops_addr + kQuadStride * (uint32_t)i);
+                            else
+                                quad_macs<kNP, true>(acc, kp, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                     ops_addr + kQuadStride * (uint32_t)i);
+                        }
                     } else {
 #pragma unroll UNR
-                        for (int i = part; i < nq; i += kLanes)
-                            quad_macs<kNP, false>(acc, kp, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
-                                                  ops_addr + kQuadStride * (uint32_t)i);
+                        for (int i = part; i < nq; i += kLanes) {
+                            if (KSM)
+                                quad_macs<kNP, false>(acc, kps, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                      ops_addr + kQuadStride * (uint32_t)i);
+                            else
+                                quad_macs<kNP, false>(acc, kp, geo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                      ops_addr + kQuadStride * (uint32_t)i);
+                        }
                     }
                     // combine the four lanes
 #pragma unroll
@@ -601,10 +621,10 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
     }
 }
 
-template <int NT, int QB, int MINB, int CB, int UNR>
+template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false>
 cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
     if (a.S % 2 != 0) return cudaErrorInvalidValue;
-    auto kern = degridder_quad_kernel<NT, QB, MINB, CB, UNR>;
+    auto kern = degridder_quad_kernel<NT, QB, MINB, CB, UNR, KSM>;
     const size_t smem = quad_layout(a.S, a.C, QB).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -623,7 +643,7 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int degridder_cp_shapes() { return 16; }
+int degridder_cp_shapes() { return 17; }
 
 // Channel-pair shapes (index within this family):
 //   0: 128 threads, 8-channel groups, 256-pixel batches, 4 CTAs/SM (16 warps)
@@ -642,11 +662,13 @@ int degridder_cp_shapes() { return 16; }
 //  13: mirror quads, 128 threads, 8-channel groups, 256-quad batches, 2 CTAs/SM
 //  14: mirror quads, 128 threads, 8-channel groups, 256-quad batches, 3 CTAs/SM (12 warps)
 //  15: shape 13 with the quad loop unrolled by two
+//  16: shape 14 reading each channel pair's kappa from shared memory when used
 cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
     case 13: return launch_quad<128, 256, 2, 8, 1>(a, stream);
     case 14: return launch_quad<128, 256, 3, 8, 1>(a, stream);
     case 15: return launch_quad<128, 256, 2, 8, 2>(a, stream);
+    case 16: return launch_quad<128, 256, 3, 8, 1, true>(a, stream);
     case 1: return launch_cp<128, 512, 3, 8, 0, 2>(a, stream);
     case 2: return launch_cp<128, 512, 2, 16, 0, 1>(a, stream);
     case 3: return launch_cp<128, 512, 3, 8, kGaussCp, 1>(a, stream);

@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Mirror-quad form (shapes 18-21).  The pixels of a subgrid come in quads
+// Mirror-quad form (shapes 18-22).  The pixels of a subgrid come in quads
 // (hx, hy), (-hx, hy), (hx, -hy), (-hx, -hy) (pixel x and S-1-x have opposite
 // hx exactly, and all four share n).  The phase of channel c is
 //   x_c = a_c hx + b_c hy + g_c n,  a_c = A + kappa_c qu, b_c = B + kappa_c qv,
@@ -895,6 +895,7 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
 //  19: mirror quads, 128 threads x 2 quads, 2 CTAs/SM (8 warps), registers uncapped
 //  20: mirror quads, 64 threads x 4 quads, 4 CTAs/SM (8 warps), unrolled by two (whole passes for S = 32)
 //  21: mirror quads, 128 threads x 4 quads, 2 CTAs/SM (8 warps), unrolled by two (whole passes for S = 64)
+//  22: shape 20 with the channel loop unrolled by four
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
 cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
@@ -936,7 +937,7 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int gridder_fast_shapes() { return 22; }
+int gridder_fast_shapes() { return 23; }
 
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
@@ -961,6 +962,7 @@ cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int sh
     case 19: return launch_quad<128, 1, 256, 2, 4>(a, stream);
     case 20: return launch_quad<64, 2, 256, 4, 2>(a, stream);
     case 21: return launch_quad<128, 2, 256, 2, 2>(a, stream);
+    case 22: return launch_quad<64, 2, 256, 4, 4>(a, stream);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
     }
 }
