@@ -31,7 +31,11 @@ std::mutex g_words_mutex;
 std::vector<DeviceWords> g_words;
 
 // Launch shapes of the batched kernels per (device, subgrid size), set by the
-// autotuner or by idg_set_batched_shapes(); shape 0 until then.
+// autotuner or by idg_set_batched_shapes().  Until then, the shapes measured
+// fastest on GB300: the mirror-quad gridder with 64 threads x 4 quads (shape
+// 22) where 64 threads cover whole quad columns (S/2 divides 64), else the
+// Gauss pixel-pair shapes that make whole passes for S = 24 (11) and 48 (12);
+// the mirror-quad degridder with kappa from shared memory (shape 31).
 std::mutex g_shape_mutex;
 std::map<std::pair<int, int>, std::pair<int, int>> g_shapes;
 
@@ -40,27 +44,34 @@ int current_device() {
     cudaGetDevice(&dev);
     return dev;
 }
+
+std::pair<int, int> default_shapes(int S) {
+    const int g = (S >= 2 && 64 % (S / 2) == 0) ? 22 : S == 24 ? 11 : S == 48 ? 12 : 13;
+    return {g < gridder_fast_shapes() ? g : 0, 31 < degridder_fast_shapes() ? 31 : 0};
+}
+
+std::pair<int, int> &shapes_of(int S) {
+    auto it = g_shapes.find({current_device(), S});
+    if (it == g_shapes.end()) it = g_shapes.emplace(std::make_pair(current_device(), S), default_shapes(S)).first;
+    return it->second;
+}
 } // namespace
 
 int batched_gridder_shape(int S) {
     std::lock_guard<std::mutex> lock(g_shape_mutex);
-    auto it = g_shapes.find({current_device(), S});
-    return it == g_shapes.end() ? 0 : it->second.first;
+    return shapes_of(S).first;
 }
 int batched_degridder_shape(int S) {
     std::lock_guard<std::mutex> lock(g_shape_mutex);
-    auto it = g_shapes.find({current_device(), S});
-    return it == g_shapes.end() ? 0 : it->second.second;
+    return shapes_of(S).second;
 }
 void set_batched_gridder_shape(int S, int shape) {
     std::lock_guard<std::mutex> lock(g_shape_mutex);
-    auto &v = g_shapes[{current_device(), S}];
-    v.first = shape;
+    shapes_of(S).first = shape;
 }
 void set_batched_degridder_shape(int S, int shape) {
     std::lock_guard<std::mutex> lock(g_shape_mutex);
-    auto &v = g_shapes[{current_device(), S}];
-    v.second = shape;
+    shapes_of(S).second = shape;
 }
 
 int fail(int code, const char *fmt, ...) {

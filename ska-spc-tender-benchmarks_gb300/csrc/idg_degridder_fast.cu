@@ -375,6 +375,7 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (a.share_den > 1) blocks = blocks / a.share_den > 0 ? blocks / a.share_den : 1;
     if (a.max_ctas > 0 && blocks > a.max_ctas) blocks = a.max_ctas;
     if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
     kern<<<(unsigned)blocks, NT, smem, stream>>>(a);

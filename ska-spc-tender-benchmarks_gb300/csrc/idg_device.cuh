@@ -119,6 +119,7 @@ struct KernelArgs {
     int *work_counter;    // batched variant: dynamic scheduler (may be NULL)
     unsigned *status;     // device check word (may be NULL)
     int max_ctas;         // persistent kernels: at most this many CTAs (0 = fill the GPU)
+    int share_den;        // persistent kernels: 1/share_den of the CTAs that fill the GPU (0, 1 = all)
 };
 
 // Plan entry after validation.

@@ -109,7 +109,6 @@ struct idg_server {
     Clock::time_point first_submit{}, last_done{};
     bool have_first = false;
     bool stop = false;
-    int full_ctas = 0; // CTAs a persistent kernel uses when it fills the GPU
     std::thread worker;
 
     void run();
@@ -208,7 +207,9 @@ void idg_server::launch(Job &j) {
     int running = 0;
     for (auto &s : slots)
         if (s) ++running;
-    a.max_ctas = (cfg.cta_share && running > 1 && full_ctas > 0) ? std::max(1, full_ctas / running) : 0;
+    // running jobs share the SMs: each persistent kernel takes 1/running of the
+    // CTAs that would fill the GPU with its own launch shape
+    a.share_den = (cfg.cta_share && running > 1) ? running : 0;
     const int variant = j.spec.variant == IDG_VARIANT_PLAIN ? IDG_VARIANT_PLAIN : IDG_VARIANT_BATCHED;
 
     // order against the other jobs on this grid
@@ -336,9 +337,6 @@ IDG_API int idg_server_create(const idg_server_config *cfg, idg_server **out) {
     auto *srv = new idg_server;
     srv->cfg = *cfg;
     cudaGetDevice(&srv->device);
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, srv->device);
-    srv->full_ctas = sms * 3;
     srv->slots.resize(cfg->max_slots);
     srv->streams.resize(cfg->max_slots);
     for (auto &s : srv->streams) {

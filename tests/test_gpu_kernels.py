@@ -295,6 +295,7 @@ def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
     vwant = oracle_mod.degridder(prm, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, obs.metadata, spec.n_rows)
     ng, nd = tuning.num_shapes()
     assert ng >= 2 and nd >= 2
+    saved = tuning.get_shapes(S)
     for sh in range(max(ng, nd)):
         tuning.set_shapes(S, min(sh, ng - 1), min(sh, nd - 1))
         got = grid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, L.VARIANT_BATCHED)
@@ -312,7 +313,7 @@ def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
     assert len(res["gridder_ms"]) == ng and all(t > 0 for t in res["gridder_ms"])
     assert tuning.get_shapes(S) == (res["gridder"], res["degridder"])
     assert res["gridder_ms"][res["gridder"]] == min(res["gridder_ms"])
-    tuning.set_shapes(S, 0, 0)
+    tuning.set_shapes(S, *saved)
 
 
 @pytest.mark.parametrize("S", [24, 48, 64])
@@ -355,6 +356,7 @@ def test_every_batched_shape_at_other_subgrid_sizes(oracle_mod, idg, S):
         covered[m["time_offset"]:m["time_offset"] + m["nr_timesteps"], e["channel_begin"]:e["channel_end"]] = True
     sp = spec_for(G, S, C, ns, obs.aterms.shape[0], image_size)
     ng, nd = tuning.num_shapes()
+    saved = tuning.get_shapes(S)
     for sh in range(max(ng, nd)):
         g_sh, d_sh = min(sh, ng - 1), min(sh, nd - 1)
         tuning.set_shapes(S, g_sh, d_sh)
@@ -365,7 +367,7 @@ def test_every_batched_shape_at_other_subgrid_sizes(oracle_mod, idg, S):
         check_rel(f"degridder S={S} shape {d_sh}", vg[covered], want_v[covered], TOL)
         assert np.all(vg[~covered] == 0)
     assert ops.device_status(clear=True) == 0
-    tuning.set_shapes(S, 0, 0)
+    tuning.set_shapes(S, *saved)
 
 
 def test_plan_steps_and_graph_cycle_match_direct_calls(oracle_mod, idg):
