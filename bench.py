@@ -112,9 +112,17 @@ def cpu_baseline(obs, vis_host: np.ndarray, target_s: float):
     S, C, T = spec.subgrid_size, spec.nchannels, spec.timesteps_per_subgrid
     md_all = obs.metadata
 
+    # the sample may only use subgrids whose rows are all in vis_host
+    row_end = md_all["time_offset"].astype(np.int64) + md_all["nr_timesteps"]
+    n_avail = int(np.searchsorted(np.maximum.accumulate(row_end), vis_host.shape[0], side="right"))
+    if n_avail < 1:
+        raise ValueError("cpu_baseline: vis_host holds no complete subgrid")
+
     def run(n, grid_too=True):
         md = md_all[:n].copy()
         rows = int(md["time_offset"][-1] + md["nr_timesteps"][-1])
+        if rows > vis_host.shape[0]:
+            raise ValueError(f"cpu_baseline: sample of {n} subgrids needs {rows} rows, vis_host has {vis_host.shape[0]}")
         prm = O.params(spec.grid_size, S, C, spec.nstations, n, spec.image_size)
         uvw = np.ascontiguousarray(obs.uvw[:rows])
         vis = np.ascontiguousarray(vis_host[:rows])
@@ -128,10 +136,10 @@ def cpu_baseline(obs, vis_host: np.ndarray, target_s: float):
         td = time.perf_counter() - t0
         return tg, td
 
-    n = 8
+    n = min(8, n_avail)
     tg, td = run(n)
     per = max((tg + td) / n, 1e-6)
-    n = int(max(8, min(spec.n_subgrids, (2 * target_s) / per)))
+    n = int(max(min(8, n_avail), min(n_avail, (2 * target_s) / per)))
     tg, td = run(n)
     nvis = n * T * C
     return {
