@@ -186,3 +186,25 @@ def test_split_plan_w_planes(idg):
     assert np.all(flat.metadata["z"] == 0)
     rest = [n for n in md.dtype.names if n != "z"]
     assert np.array_equal(flat.metadata[rest], md[rest]) and np.array_equal(flat.ext, ext)
+
+
+def test_cpu_baseline_sample_stays_within_the_given_rows(idg):
+    """The bench's CPU baseline sizes its sample from the measured time per
+    subgrid; however fast the host, the sample only uses subgrids whose rows
+    are all in the visibilities it was given (a faster host once read past
+    them)."""
+    import importlib.util
+    import os
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec_b = importlib.util.spec_from_file_location("bench_under_test", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec_b)
+    spec_b.loader.exec_module(bench)
+    from idg_gb300 import datasets as D
+
+    spec = D.config1()
+    obs = D.make_observation(spec)
+    T = spec.timesteps_per_subgrid
+    vis = np.zeros((5 * T + T // 2, spec.nchannels, 4), np.complex64)  # 5 whole subgrids and part of a sixth
+    out = bench.cpu_baseline(obs, vis, 1000.0)
+    assert out["sample"].startswith("first 5 of ")
