@@ -30,7 +30,6 @@ namespace idg {
 
 namespace {
 
-constexpr int kMaxTileVis = 256;              // visibilities per staged tile, at most
 constexpr int kMaxTT = 64;                    // timesteps per tile, at most
 constexpr float kFastBound = 48.f;            // radians
 constexpr uint64_t kWaitNs = 2000000000ull;   // a staged copy not complete after 2 s is declared lost
@@ -328,6 +327,59 @@ __device__ inline void build_chains(const f2 *kap, ChainInfo *chains, int nc, in
     }
 }
 
+// One staged tile of a batched gridder.  Thread 0 issues one bulk copy per
+// row (tt rows x ncc visibilities from channel c0 + cb) onto the mbarrier;
+// meanwhile all threads compute the per-timestep phase coefficients (FP64,
+// offsets reduced, stored as float pairs) and fold the tile's phase-slope
+// bound into head->qmax_bits: the sum of the three slopes (QSUM, one phase
+// per pixel) or their maximum (the factored forms, one argument per factor).
+// Then the bounded wait.  Returns false when the copies did not arrive: the
+// abort flag and the status bit are set, and the CTA must stop.
+template <int NT, bool QSUM>
+__device__ __forceinline__ bool stage_tile(const KernelArgs &a, const SubgridInfo &si, SmemHead *head, float4 *raw,
+                                           float4 *coef, int t0, int tt, int cb, int ncc, double kref, double d2pi,
+                                           float hmax, float nmax, uint32_t &phase) {
+    const int tid = threadIdx.x, S = a.S;
+    __syncthreads(); // previous tile fully consumed (raw, expanded operands, coef)
+    if (tid == 0) {
+        const uint32_t row_bytes = (uint32_t)ncc * 32u;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&head->bar, row_bytes * (uint32_t)tt);
+        const float4 *src = a.vis + ((int64_t)si.row0 + t0) * a.C * 2 + (int64_t)(si.c0 + cb) * 2;
+        for (int r = 0; r < tt; ++r)
+            bulk_g2s(raw + (size_t)r * ncc * 2, src + (int64_t)r * a.C * 2, row_bytes, &head->bar);
+    }
+    for (int t = tid; t < tt; t += NT) {
+        const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
+        const double u = p[0], v = p[1], w = p[2];
+        double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
+        double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
+        ca -= 2.0 * rint(ca * 0.5);
+        cbv -= 2.0 * rint(cbv * 0.5);
+        const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
+        const float A = (float)(kTwoPi * ca), B = (float)(kTwoPi * cbv), Gv = (float)cg;
+        const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
+        coef[3 * t + 0] = make_float4(A, A, B, B);
+        coef[3 * t + 1] = make_float4(Gv, Gv, qu, qu);
+        coef[3 * t + 2] = make_float4(qv, qv, qw, qw);
+        const float qm = QSUM ? fabsf(qu) * hmax + fabsf(qv) * hmax + fabsf(qw) * nmax
+                              : fmaxf(fmaxf(fabsf(qu) * hmax, fabsf(qv) * hmax), fabsf(qw) * nmax);
+        atomicMax(&head->qmax_bits, __float_as_int(qm));
+    }
+    if (!mbar_wait_bounded(&head->bar, phase, kWaitNs)) {
+        head->abort = 1;
+        flag_status(a.status, kStatusTimeout);
+    }
+    __syncthreads();
+    if (head->abort) {
+        // give the copies in flight one more bounded wait before the CTA exits
+        if (tid == 0) mbar_wait_bounded(&head->bar, phase, kWaitNs);
+        return false;
+    }
+    phase ^= 1u;
+    return true;
+}
+
 // Kernel shape: NT threads per CTA, PAIRS pixel pairs per thread per pass,
 // TV visibilities per staged tile, at least MINB CTAs per SM (register cap).
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
@@ -422,45 +474,9 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
                 const int ncc = min(chunk, nc - cb);
                 for (int t0 = 0; t0 < si.T; t0 += TT) {
                     const int tt = min(TT, si.T - t0);
-                    // ---- stage: bulk copies of tt rows x ncc visibilities
-                    __syncthreads(); // previous tile fully consumed (raw, vexp, coef)
-                    if (tid == 0) {
-                        const uint32_t row_bytes = (uint32_t)ncc * 32u;
-                        fence_proxy_async();
-                        mbar_arrive_expect_tx(&head->bar, row_bytes * (uint32_t)tt);
-                        const float4 *src = a.vis + ((int64_t)si.row0 + t0) * a.C * 2 + (int64_t)(si.c0 + cb) * 2;
-                        for (int r = 0; r < tt; ++r)
-                            bulk_g2s(raw + (size_t)r * ncc * 2, src + (int64_t)r * a.C * 2, row_bytes, &head->bar);
-                    }
-                    // phase coefficients (FP64) for the tile's timesteps, and max |Q|
-                    for (int t = tid; t < tt; t += kT) {
-                        const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
-                        const double u = p[0], v = p[1], w = p[2];
-                        double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
-                        double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
-                        ca -= 2.0 * rint(ca * 0.5);
-                        cbv -= 2.0 * rint(cbv * 0.5);
-                        const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
-                        const float A = (float)(kTwoPi * ca), B = (float)(kTwoPi * cbv), Gv = (float)cg;
-                        const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
-                        coef[3 * t + 0] = make_float4(A, A, B, B);
-                        coef[3 * t + 1] = make_float4(Gv, Gv, qu, qu);
-                        coef[3 * t + 2] = make_float4(qv, qv, qw, qw);
-                        const float qm = fabsf(qu) * hmax + fabsf(qv) * hmax + fabsf(qw) * nmax;
-                        atomicMax(&head->qmax_bits, __float_as_int(qm));
-                    }
-                    // ---- wait for the copies, expand into operand pairs
-                    if (!mbar_wait_bounded(&head->bar, phase, kWaitNs)) {
-                        head->abort = 1;
-                        flag_status(a.status, kStatusTimeout);
-                    }
-                    __syncthreads();
-                    if (head->abort) {
-                        // give the copies in flight one more bounded wait before the CTA exits
-                        if (tid == 0) mbar_wait_bounded(&head->bar, phase, kWaitNs);
+                    // ---- stage the tile, then expand into operand pairs
+                    if (!stage_tile<kT, true>(a, si, head, raw, coef, t0, tt, cb, ncc, kref, d2pi, hmax, nmax, phase))
                         break;
-                    }
-                    phase ^= 1u;
                     for (int i = tid; i < tt * ncc; i += kT) {
                         const float4 v0 = raw[2 * i], v1 = raw[2 * i + 1];
                         float4 *d = vexp + 6 * i;
@@ -758,41 +774,8 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
                 const int ncc = min(chunk, nc - cb);
                 for (int t0 = 0; t0 < si.T; t0 += TT) {
                     const int tt = min(TT, si.T - t0);
-                    __syncthreads(); // previous tile fully consumed (raw, vq, coef)
-                    if (tid == 0) {
-                        const uint32_t row_bytes = (uint32_t)ncc * 32u;
-                        fence_proxy_async();
-                        mbar_arrive_expect_tx(&head->bar, row_bytes * (uint32_t)tt);
-                        const float4 *src = a.vis + ((int64_t)si.row0 + t0) * a.C * 2 + (int64_t)(si.c0 + cb) * 2;
-                        for (int r = 0; r < tt; ++r)
-                            bulk_g2s(raw + (size_t)r * ncc * 2, src + (int64_t)r * a.C * 2, row_bytes, &head->bar);
-                    }
-                    for (int t = tid; t < tt; t += kT) {
-                        const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
-                        const double u = p[0], v = p[1], w = p[2];
-                        double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
-                        double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
-                        ca -= 2.0 * rint(ca * 0.5);
-                        cbv -= 2.0 * rint(cbv * 0.5);
-                        const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
-                        const float A = (float)(kTwoPi * ca), B = (float)(kTwoPi * cbv), Gv = (float)cg;
-                        const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
-                        coef[3 * t + 0] = make_float4(A, A, B, B);
-                        coef[3 * t + 1] = make_float4(Gv, Gv, qu, qu);
-                        coef[3 * t + 2] = make_float4(qv, qv, qw, qw);
-                        const float qm = fmaxf(fmaxf(fabsf(qu) * hmax, fabsf(qv) * hmax), fabsf(qw) * nmax);
-                        atomicMax(&head->qmax_bits, __float_as_int(qm));
-                    }
-                    if (!mbar_wait_bounded(&head->bar, phase, kWaitNs)) {
-                        head->abort = 1;
-                        flag_status(a.status, kStatusTimeout);
-                    }
-                    __syncthreads();
-                    if (head->abort) {
-                        if (tid == 0) mbar_wait_bounded(&head->bar, phase, kWaitNs);
+                    if (!stage_tile<kT, false>(a, si, head, raw, coef, t0, tt, cb, ncc, kref, d2pi, hmax, nmax, phase))
                         break;
-                    }
-                    phase ^= 1u;
                     // expand: per visibility and correlation (re, re, im, im)
                     for (int i = tid; i < tt * ncc; i += kT) {
                         const float4 v0 = raw[2 * i], v1 = raw[2 * i + 1];
