@@ -128,6 +128,76 @@ __device__ __forceinline__ void group_pixels(f2 (&acc)[NPAIR][NACC], const f2 (&
     }
 }
 
+// Per-timestep phase coefficients of one time tile (FP64, offsets reduced,
+// stored as floats: (a, b, g, qu) (qv, qw, -, -)), and the tile's decision for
+// the unreduced sincos: the phase-slope bound is the sum of the three slopes
+// (QSUM, one phase per pixel) or their maximum (the factored quad form).
+// Contains the tile's barriers; returns the decision.
+template <int NT, bool QSUM>
+__device__ __forceinline__ bool tile_coefficients(const KernelArgs &a, const SubgridInfo &si, Head *head,
+                                                  float4 *coef, int t0, int tt, double kref, double d2pi, float hmax,
+                                                  float nmax) {
+    const int tid = threadIdx.x, S = a.S;
+    __syncthreads();
+    for (int t = tid; t < tt; t += NT) {
+        const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
+        const double u = p[0], v = p[1], w = p[2];
+        double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
+        double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
+        ca -= 2.0 * rint(ca * 0.5);
+        cbv -= 2.0 * rint(cbv * 0.5);
+        const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
+        const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
+        coef[2 * t + 0] = make_float4((float)(kTwoPi * ca), (float)(kTwoPi * cbv), (float)cg, qu);
+        coef[2 * t + 1] = make_float4(qv, qw, 0.f, 0.f);
+        const float qm = QSUM ? fabsf(qu) * hmax + fabsf(qv) * hmax + fabsf(qw) * nmax
+                              : fmaxf(fmaxf(fabsf(qu) * hmax, fabsf(qv) * hmax), fabsf(qw) * nmax);
+        atomicMax(&head->qmax_bits, __float_as_int(qm));
+    }
+    __syncthreads();
+    if (tid == 0) {
+        head->fast = (3.1416f + __int_as_float(head->kmax_bits) * __int_as_float(head->qmax_bits)) <= kFastBound;
+        head->qmax_bits = 0;
+    }
+    __syncthreads();
+    return head->fast != 0;
+}
+
+// Writes a visibility group's combined sums: lane `part` stores the channel
+// pairs j = part, part + 4, ... of the group (out[j][r]: correlation r / 2,
+// re / im for r even / odd, the two channels in the halves), adding to the
+// row when an earlier pixel batch of the subgrid already wrote it.
+template <int NP>
+__device__ __forceinline__ void write_group(const KernelArgs &a, const SubgridInfo &si, int t_abs, int cfirst, int nc,
+                                            int part, bool accumulate, const f2 (&out)[NP][8]) {
+    float4 *row = a.vis + (int64_t)t_abs * a.C * 2;
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+        if (j % kLanes != part) continue;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (cfirst + 2 * j + h >= nc) continue;
+            const int c = si.c0 + cfirst + 2 * j + h;
+            float w[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                float lo, hi;
+                unpack2(out[j][r], lo, hi);
+                w[r] = h ? hi : lo;
+            }
+            float4 va = make_float4(w[0], w[1], w[2], w[3]);
+            float4 vb = make_float4(w[4], w[5], w[6], w[7]);
+            if (accumulate) {
+                const float4 oa = row[2 * c], ob = row[2 * c + 1];
+                va = make_float4(va.x + oa.x, va.y + oa.y, va.z + oa.z, va.w + oa.w);
+                vb = make_float4(vb.x + ob.x, vb.y + ob.y, vb.z + ob.z, vb.w + ob.w);
+            }
+            row[2 * c] = va;
+            row[2 * c + 1] = vb;
+        }
+    }
+}
+
 // NT threads, BATCH pixels staged per pass, at least MINB CTAs per SM, CB
 // channels per group (8 or 16), FLAGS: kGaussCp; UNR: pixel-loop unrolling.
 template <int NT, int BATCH, int MINB, int CB, int FLAGS, int UNR>
@@ -230,27 +300,7 @@ __global__ void __launch_bounds__(NT, MINB) degridder_cp_kernel(KernelArgs a) {
 
             for (int t0 = 0; t0 < si.T; t0 += kTimeTile) {
                 const int tt = min(kTimeTile, si.T - t0);
-                __syncthreads();
-                for (int t = tid; t < tt; t += kT) {
-                    const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
-                    const double u = p[0], v = p[1], w = p[2];
-                    double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
-                    double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
-                    ca -= 2.0 * rint(ca * 0.5);
-                    cbv -= 2.0 * rint(cbv * 0.5);
-                    const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
-                    const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
-                    coef[2 * t + 0] = make_float4((float)(kTwoPi * ca), (float)(kTwoPi * cbv), (float)cg, qu);
-                    coef[2 * t + 1] = make_float4(qv, qw, 0.f, 0.f);
-                    atomicMax(&head->qmax_bits, __float_as_int(fabsf(qu) * hmax + fabsf(qv) * hmax + fabsf(qw) * nmax));
-                }
-                __syncthreads();
-                if (tid == 0) {
-                    head->fast = (3.1416f + __int_as_float(head->kmax_bits) * __int_as_float(head->qmax_bits)) <= kFastBound;
-                    head->qmax_bits = 0;
-                }
-                __syncthreads();
-                const bool fast = head->fast != 0;
+                const bool fast = tile_coefficients<kT, true>(a, si, head, coef, t0, tt, kref, d2pi, hmax, nmax);
                 const int ngroups = tt * ncb;
                 for (int gbase = warp * kGroupsPerWarp; gbase < ngroups; gbase += (kT / 32) * kGroupsPerWarp) {
                     const int grp = gbase + gw;
@@ -283,34 +333,7 @@ __global__ void __launch_bounds__(NT, MINB) degridder_cp_kernel(KernelArgs a) {
                             v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 2));
                             out[j][r] = v;
                         }
-                    if (active) {
-                        float4 *row = a.vis + ((int64_t)si.row0 + t0 + t) * a.C * 2;
-#pragma unroll
-                        for (int j = 0; j < kNP; ++j) {
-                            if (j % kLanes != part) continue;
-#pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                if (cfirst + 2 * j + h >= nc) continue;
-                                const int c = si.c0 + cfirst + 2 * j + h;
-                                float w[8];
-#pragma unroll
-                                for (int r = 0; r < 8; ++r) {
-                                    float lo, hi;
-                                    unpack2(out[j][r], lo, hi);
-                                    w[r] = h ? hi : lo;
-                                }
-                                float4 va = make_float4(w[0], w[1], w[2], w[3]);
-                                float4 vb = make_float4(w[4], w[5], w[6], w[7]);
-                                if (pb > 0) {
-                                    const float4 oa = row[2 * c], ob = row[2 * c + 1];
-                                    va = make_float4(va.x + oa.x, va.y + oa.y, va.z + oa.z, va.w + oa.w);
-                                    vb = make_float4(vb.x + ob.x, vb.y + ob.y, vb.z + ob.z, vb.w + ob.w);
-                                }
-                                row[2 * c] = va;
-                                row[2 * c + 1] = vb;
-                            }
-                        }
-                    }
+                    if (active) write_group<kNP>(a, si, si.row0 + t0 + t, cfirst, nc, part, pb > 0, out);
                 }
             }
         }
@@ -374,7 +397,6 @@ __host__ __device__ inline QuadLayout quad_layout(int S, int C, int batch) {
 // KP: the channel pairs' kappa, either f2 registers (f2[NPAIR]) or a pointer
 // to the group's first channel in shared memory (read per channel pair).
 __device__ __forceinline__ f2 kappa_pair(const f2 (&kp)[4], int j) { return kp[j]; }
-__device__ __forceinline__ f2 kappa_pair(const f2 (&kp)[8], int j) { return kp[j]; }
 __device__ __forceinline__ f2 kappa_pair(const float *kp, int j) {
     return *reinterpret_cast<const f2 *>(kp + 2 * j);
 }
@@ -515,28 +537,7 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
 
             for (int t0 = 0; t0 < si.T; t0 += kTimeTile) {
                 const int tt = min(kTimeTile, si.T - t0);
-                __syncthreads();
-                for (int t = tid; t < tt; t += kT) {
-                    const float *p = a.uvw + 3 * ((int64_t)si.row0 + t0 + t);
-                    const double u = p[0], v = p[1], w = p[2];
-                    double ca = ((double)si.X + S * 0.5 - a.G * 0.5) / S - kref * u * d2pi;
-                    double cbv = ((double)si.Y + S * 0.5 - a.G * 0.5) / S - kref * v * d2pi;
-                    ca -= 2.0 * rint(ca * 0.5);
-                    cbv -= 2.0 * rint(cbv * 0.5);
-                    const double cg = kTwoPi * (double)a.w_step * ((double)si.Z + 0.5) - kref * w;
-                    const float qu = (float)(-u * d2pi * kTwoPi), qv = (float)(-v * d2pi * kTwoPi), qw = (float)(-w);
-                    coef[2 * t + 0] = make_float4((float)(kTwoPi * ca), (float)(kTwoPi * cbv), (float)cg, qu);
-                    coef[2 * t + 1] = make_float4(qv, qw, 0.f, 0.f);
-                    const float qm = fmaxf(fmaxf(fabsf(qu) * hmax, fabsf(qv) * hmax), fabsf(qw) * nmax);
-                    atomicMax(&head->qmax_bits, __float_as_int(qm));
-                }
-                __syncthreads();
-                if (tid == 0) {
-                    head->fast = (3.1416f + __int_as_float(head->kmax_bits) * __int_as_float(head->qmax_bits)) <= kFastBound;
-                    head->qmax_bits = 0;
-                }
-                __syncthreads();
-                const bool fast = head->fast != 0;
+                const bool fast = tile_coefficients<kT, false>(a, si, head, coef, t0, tt, kref, d2pi, hmax, nmax);
                 const int ngroups = tt * ncb;
                 for (int gbase = warp * kGroupsPerWarp; gbase < ngroups; gbase += (kT / 32) * kGroupsPerWarp) {
                     const int grp = gbase + gw;
@@ -575,6 +576,7 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
                         }
                     }
                     // combine the four lanes
+                    f2 out[kNP][8];
 #pragma unroll
                     for (int j = 0; j < kNP; ++j)
 #pragma unroll
@@ -584,38 +586,9 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
                                 f2 v = acc[j][k][r];
                                 v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 1));
                                 v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 2));
-                                acc[j][k][r] = v;
+                                out[j][2 * k + r] = v;
                             }
-                    if (active) {
-                        float4 *row = a.vis + ((int64_t)si.row0 + t0 + t) * a.C * 2;
-#pragma unroll
-                        for (int j = 0; j < kNP; ++j) {
-                            if (j % kLanes != part) continue;
-#pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                if (cfirst + 2 * j + h >= nc) continue;
-                                const int c = si.c0 + cfirst + 2 * j + h;
-                                float w[8];
-#pragma unroll
-                                for (int k = 0; k < 4; ++k)
-#pragma unroll
-                                    for (int r = 0; r < 2; ++r) {
-                                        float lo, hi;
-                                        unpack2(acc[j][k][r], lo, hi);
-                                        w[2 * k + r] = h ? hi : lo;
-                                    }
-                                float4 va = make_float4(w[0], w[1], w[2], w[3]);
-                                float4 vb = make_float4(w[4], w[5], w[6], w[7]);
-                                if (qb > 0) {
-                                    const float4 oa = row[2 * c], ob = row[2 * c + 1];
-                                    va = make_float4(va.x + oa.x, va.y + oa.y, va.z + oa.z, va.w + oa.w);
-                                    vb = make_float4(vb.x + ob.x, vb.y + ob.y, vb.z + ob.z, vb.w + ob.w);
-                                }
-                                row[2 * c] = va;
-                                row[2 * c + 1] = vb;
-                            }
-                        }
-                    }
+                    if (active) write_group<kNP>(a, si, si.row0 + t0 + t, cfirst, nc, part, qb > 0, out);
                 }
             }
         }
