@@ -208,3 +208,26 @@ def test_cpu_baseline_sample_stays_within_the_given_rows(idg):
     vis = np.zeros((5 * T + T // 2, spec.nchannels, 4), np.complex64)  # 5 whole subgrids and part of a sixth
     out = bench.cpu_baseline(obs, vis, 1000.0)
     assert out["sample"].startswith("first 5 of ")
+
+
+def test_e2e_leg_fits_the_host_memory(idg):
+    """bench.py's e2e leg pins the visibilities in and out per rank; with too
+    little host memory for all ranks of a node it takes the leading subgrids
+    whose rows fit (whole plan otherwise)."""
+    import importlib.util
+    import os
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec_b = importlib.util.spec_from_file_location("bench_under_test2", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec_b)
+    spec_b.loader.exec_module(bench)
+    from idg_gb300 import datasets as D
+
+    spec = D.config1()
+    obs = D.make_observation(spec)
+    row = 2 * spec.nchannels * 32
+    assert bench.e2e_prefix(obs.metadata, spec.n_rows, row, 1e18) == (spec.n_subgrids, spec.n_rows)
+    T = spec.timesteps_per_subgrid
+    n, rows = bench.e2e_prefix(obs.metadata, spec.n_rows, row, (3 * T + T // 2) * row)
+    assert (n, rows) == (3, 3 * T)
+    assert bench.e2e_prefix(obs.metadata, spec.n_rows, row, 1.0)[0] == 1
