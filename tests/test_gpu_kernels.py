@@ -418,3 +418,62 @@ def test_plan_steps_and_graph_cycle_match_direct_calls(oracle_mod, idg):
         check_rel(f"graph cycle vis v{variant}", v2.cpu().numpy(), v_ref.cpu().numpy(), TOL)
         assert plan.status() == 0
         plan.close()
+
+
+def test_degenerate_plan_entries_every_batched_shape(oracle_mod, idg):
+    """Every batched launch shape on plan entries at the edges of what a plan may
+    hold: zero and one timestep, empty and one-channel ranges, ranges starting
+    at odd channels, subgrids at the grid's edges.  Gridder outputs equal the
+    FP64 oracle (zeros where nothing is gridded); the degridder writes exactly
+    the covered samples and leaves the others at zero."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops, tuning
+
+    rng = np.random.default_rng(321)
+    G, C, ns, S = 1024, 12, 4, 32
+    image_size = 0.04
+    spec = D.ObservationSpec(nstations=ns, disk_radius_m=2000.0, ntimesteps=64, timesteps_per_subgrid=64,
+                             nchannels=C, f_start=140e6, f_end=170e6, subgrid_size=S, grid_size=G,
+                             image_size=image_size, aterm_sigma=0.05, seed=11)
+    obs = D.make_observation(spec)
+    T = np.array([0, 1, 2, 3, 1, 5, 0, 7, 2, 1])
+    lens = np.array([4, 0, 1, 12, 1, 3, 0, 2, 11, 1])
+    c0 = np.array([0, 5, 11, 0, 7, 9, 3, 1, 1, 0])
+    N = len(T)
+    md = np.zeros(N, L.METADATA_DTYPE)
+    md["time_offset"] = np.concatenate([[0], np.cumsum(T)[:-1]])
+    md["nr_timesteps"] = T
+    md["station1"] = rng.integers(0, ns - 1, N)
+    md["station2"] = md["station1"] + 1
+    md["x"] = np.array([0, G - S, 3, 17, G - S, 400, 0, 9, 511, G // 2 - S // 2])
+    md["y"] = np.array([G - S, 0, 0, 500, G - S, 8, 0, 31, 2, G // 2 - S // 2])
+    ext = np.zeros(N, L.SUBGRID_EXT_DTYPE)
+    ext["channel_begin"] = c0
+    ext["channel_end"] = c0 + lens
+    rows = int(T.sum())
+    uvw = np.ascontiguousarray(obs.uvw[:rows])
+    vis = (rng.standard_normal((rows, C, 4)) + 1j * rng.standard_normal((rows, C, 4))).astype(np.complex64)
+    sub_in = (rng.standard_normal((N, 4, S, S)) + 1j * rng.standard_normal((N, 4, S, S))).astype(np.complex64)
+    want_g, want_v = _oracle_with_ext(oracle_mod, G, S, ns, image_size, uvw, obs.wavenumbers, vis, obs.taper,
+                                      obs.aterms, md, ext, sub_in)
+    covered = np.zeros((rows, C), bool)
+    for m, e in zip(md, ext):
+        covered[m["time_offset"]:m["time_offset"] + m["nr_timesteps"], e["channel_begin"]:e["channel_end"]] = True
+    empty = (T == 0) | (lens == 0)
+    sp = spec_for(G, S, C, ns, obs.aterms.shape[0], image_size)
+    ng, nd = tuning.num_shapes()
+    saved = tuning.get_shapes(S)
+    try:
+        for sh in range(max(ng, nd)):
+            g_sh, d_sh = min(sh, ng - 1), min(sh, nd - 1)
+            tuning.set_shapes(S, g_sh, d_sh)
+            got = grid_gpu(sp, md, uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, L.VARIANT_BATCHED, ext=ext)
+            assert np.all(got[empty] == 0), g_sh
+            check_rel(f"degenerate entries gridder shape {g_sh}", got[~empty], want_g[~empty], TOL)
+            vg = degrid_gpu(sp, md, uvw, obs.wavenumbers, sub_in, obs.taper, obs.aterms, rows, L.VARIANT_BATCHED,
+                            ext=ext)
+            check_rel(f"degenerate entries degridder shape {d_sh}", vg[covered], want_v[covered], TOL)
+            assert np.all(vg[~covered] == 0), d_sh
+        assert ops.device_status(clear=True) == 0
+    finally:
+        tuning.set_shapes(S, *saved)
