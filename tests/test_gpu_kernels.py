@@ -316,7 +316,7 @@ def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
     tuning.set_shapes(S, *saved)
 
 
-@pytest.mark.parametrize("S", [24, 48, 64])
+@pytest.mark.parametrize("S", [8, 16, 24, 48, 64])
 def test_every_batched_shape_at_other_subgrid_sizes(oracle_mod, idg, S):
     """Every launch shape of both batched kernels (pixel-pair and channel-pair
     degridders included) on an uneven plan with subgrid sizes that need partial
