@@ -124,18 +124,18 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
     __shared__ float2 tw[S];      // e^{+2 pi i m / S}
     __shared__ float2 post[S];    // c_j = (-1)^j e^{+i pi (j - S/2)/S}
     __shared__ float2 buf[Sh::planes][S][Sh::pitch];
-    __shared__ float tp[S * S];   // taper (ones when none is given)
     constexpr int kBatch = 8;     // 16-byte loads in flight per thread
 
     const int tid = threadIdx.x;
-    for (int q = tid; q < S * S; q += Sh::threads) tp[q] = taper ? taper[q] : 1.f;
     if (tid < S) {
-        double s, c;
-        sincospi(2.0 * tid / S, &s, &c);
-        tw[tid] = make_float2((float)c, (float)s);
-        sincospi((tid - S * 0.5) / S, &s, &c);
-        const double sg = (tid & 1) ? -1.0 : 1.0;
-        post[tid] = make_float2((float)(sg * c), (float)(sg * s));
+        // single-precision sincospi: a unit in the last place, far inside the
+        // transform's tolerance, and no FP64 work in every CTA
+        float s, c;
+        sincospif(2.0f * (float)tid / (float)S, &s, &c);
+        tw[tid] = make_float2(c, s);
+        sincospif(((float)tid - 0.5f * (float)S) / (float)S, &s, &c);
+        const float sg = (tid & 1) ? -1.f : 1.f;
+        post[tid] = make_float2(sg * c, sg * s);
     }
     const int64_t plane0 = (int64_t)blockIdx.x * Sh::planes;
     const int nplanes = (int)min((int64_t)Sh::planes, nr_planes - plane0);
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
                 const int pl = e / (S * S), q = e - pl * S * S, y = q / S, x = q - y * S;
                 float2 w = h ? make_float2(v[k].z, v[k].w) : make_float2(v[k].x, v[k].y);
                 if (DIR > 0) {
-                    const float f = (((x + y) & 1) ? -1.f : 1.f) * tp[q];
+                    const float f = (((x + y) & 1) ? -1.f : 1.f) * (taper ? __ldg(taper + q) : 1.f);
                     w = make_float2(w.x * f, w.y * f);
                 } else {
                     const float2 cy = post[y], cx = post[x];
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
                 const cf r2 = cmul(cmul({v.x, v.y}, {cy.x, cy.y}), {cx.x, cx.y});
                 v = make_float2(r2.re, r2.im);
             } else {
-                const float f = (((xx + y) & 1) ? -1.f : 1.f) * tp[q];
+                const float f = (((xx + y) & 1) ? -1.f : 1.f) * (taper ? __ldg(taper + q) : 1.f);
                 v = make_float2(v.x * f, v.y * f);
             }
             o[h] = v;
