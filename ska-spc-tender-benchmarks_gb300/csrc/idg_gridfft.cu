@@ -13,10 +13,11 @@
 //
 // Passes per plane: row FFTs, tiled transpose, row FFTs, tiled transpose.  A
 // row FFT runs in one CTA: the row is staged in shared memory and transformed
-// by radix-4 Stockham stages (plus one radix-2 stage when log2 G is odd),
-// ping-ponging between two shared buffers; twiddles come from a table of
-// e^{-2 pi i m / G} computed in FP64 on the host and staged in shared memory
-// with the row.  All passes are HBM-bound:
+// by radix-16 Stockham passes in registers (the last one of radix 2, 4 or 8
+// when log2 G is not a multiple of 4), ping-ponging between two shared
+// buffers; twiddles come from a table of
+// e^{-2 pi i m / G} computed in FP64 on the host, read through the read-only
+// cache (one table serves every row of the pass).  All passes are HBM-bound:
 // 16 bytes per complex cell per pass (read + write).
 #include <cmath>
 #include <map>
@@ -37,29 +38,124 @@ constexpr int kTile = 32;
 __device__ __forceinline__ float2 cm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
+// Shared-memory layout of a staged row: one float2 of padding after every 16,
+// so that a thread's 16 consecutive outputs of the first pass, and the
+// column-strided inputs of every pass, fall in distinct banks.
+__device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
+
+// cos / sin of 2 pi m / 16 (compile-time constants once m is).
+__host__ __device__ constexpr float kcos16(int m) {
+    constexpr float t[16] = {1.f, 0.92387953251128674f, 0.70710678118654752f, 0.38268343236508977f,
+                             0.f, -0.38268343236508977f, -0.70710678118654752f, -0.92387953251128674f,
+                             -1.f, -0.92387953251128674f, -0.70710678118654752f, -0.38268343236508977f,
+                             0.f, 0.38268343236508977f, 0.70710678118654752f, 0.92387953251128674f};
+    return t[m & 15];
+}
+__host__ __device__ constexpr float ksin16(int m) { return kcos16(m - 4); }
+
+__host__ __device__ constexpr int brev(int i, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+
+// y[j] = sum_r x[r] e^{SIGN 2 pi i r j / M} in registers, M in {2, 4, 8, 16}:
+// bit-reversal permutation, then radix-2 decimation-in-time stages with
+// compile-time twiddles.
+template <int M, int SIGN, int I = 0>
+__device__ __forceinline__ void brev_perm(float2 (&x)[M]) {
+    if constexpr (I < M) {
+        constexpr int J = brev(I, M == 2 ? 1 : M == 4 ? 2 : M == 8 ? 3 : 4);
+        if constexpr (J > I) {
+            const float2 t = x[I];
+            x[I] = x[J];
+            x[J] = t;
+        }
+        brev_perm<M, SIGN, I + 1>(x);
+    }
+}
+template <int M, int SIGN, int LEN = 2>
+__device__ __forceinline__ void dit_stages(float2 (&x)[M]) {
+    if constexpr (LEN <= M) {
+#pragma unroll
+        for (int i0 = 0; i0 < M; i0 += LEN) {
+#pragma unroll
+            for (int j = 0; j < LEN / 2; ++j) {
+                const float2 u = x[i0 + j];
+                float2 v = x[i0 + j + LEN / 2];
+                if (j > 0) v = cm(v, make_float2(kcos16(j * (16 / LEN)), SIGN * ksin16(j * (16 / LEN))));
+                x[i0 + j] = make_float2(u.x + v.x, u.y + v.y);
+                x[i0 + j + LEN / 2] = make_float2(u.x - v.x, u.y - v.y);
+            }
+        }
+        dit_stages<M, SIGN, 2 * LEN>(x);
+    }
+}
+
+// One Stockham pass of radix R over sub-length L (the product of the radices
+// before it): butterfly b = (q, k), k = b mod L, reads elements b + r G/R,
+// twiddles element r by e^{DIR 2 pi i r k / (L R)} (table e^{-2 pi i m / G},
+// conjugated for DIR = +1), transforms the R values in registers and writes
+// them to q L R + k + r L.
+template <int DIR, int G, int L, int R>
+__device__ __forceinline__ void stockham_pass(const float2 *src, float2 *dst, const float2 *tw_g) {
+    constexpr int n = G / (L * R);
+    for (int b = threadIdx.x; b < G / R; b += kRowThreads) {
+        const int k = b % L, q = b / L;
+        float2 x[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) x[r] = src[pad16(b + r * (G / R))];
+        if (L > 1 && k > 0) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                const float2 w = __ldg(tw_g + (r * k) * n);
+                x[r] = cm(x[r], DIR < 0 ? w : conjf2(w));
+            }
+        }
+        brev_perm<R, DIR>(x);
+        dit_stages<R, DIR>(x);
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[pad16(q * L * R + k + r * L)] = x[r];
+    }
+}
+
+// The passes of a length-G transform: radix 16 while at least 16 points of
+// the length are left, then one pass of radix 2, 4 or 8.  Swaps src / dst
+// after every pass, so the result is in src at the end.
+template <int DIR, int G, int L>
+__device__ __forceinline__ void stockham_passes(float2 *&src, float2 *&dst, const float2 *tw_g) {
+    if constexpr (L < G) {
+        constexpr int rem = G / L, R = rem >= 16 ? 16 : rem;
+        stockham_pass<DIR, G, L, R>(src, dst, tw_g);
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+        stockham_passes<DIR, G, L * R>(src, dst, tw_g);
+    }
+}
+
 // One FFT over the CTA's row (length G = 2^LOGG, row stride G).  DIR = -1
 // uses e^{-2 pi i ...}, DIR = +1 its conjugate.  Element i of the row is
 // multiplied by (-1)^i before and after the transform (the centre shifts of
 // this dimension), and by corr[i] (when given) after it for DIR = -1 or before
-// it for DIR = +1.  The row and the twiddle table are staged in shared memory
-// with all of a thread's 16-byte loads issued before any is used.
+// it for DIR = +1.  The row is staged in padded shared memory with all of a
+// thread's 16-byte loads issued before any is used, then transformed by
+// radix-16 Stockham passes in registers (three for G = 4096).
 template <int DIR, int LOGG>
 __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data, const float2 *tw_g,
                                                                    const float *corr) {
     constexpr int G = 1 << LOGG, kVec = G / 2;  // float4 per row
     constexpr int kPer = (kVec + kRowThreads - 1) / kRowThreads;
     extern __shared__ float2 sm[];
-    float2 *A = sm, *B = sm + G, *tw = sm + 2 * G;
+    float2 *A = sm, *B = sm + (G + G / 16);
     const int row = blockIdx.x;
     float2 *p = data + (int64_t)row * G;
-    float4 v[kPer], t[kPer];
+    float4 v[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
         const int i2 = threadIdx.x + k * kRowThreads;
-        if (i2 < kVec) {
-            v[k] = reinterpret_cast<const float4 *>(p)[i2];
-            t[k] = reinterpret_cast<const float4 *>(tw_g)[i2];
-        }
+        if (i2 < kVec) v[k] = reinterpret_cast<const float4 *>(p)[i2];
     }
     // pre-multiply for the image -> uv direction
 #pragma unroll
@@ -71,70 +167,18 @@ __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data,
             fa *= corr[2 * i2];
             fb *= corr[2 * i2 + 1];
         }
-        A[2 * i2] = make_float2(v[k].x * fa, v[k].y * fa);
-        A[2 * i2 + 1] = make_float2(v[k].z * fb, v[k].w * fb);
-        reinterpret_cast<float4 *>(tw)[i2] = t[k];
+        A[pad16(2 * i2)] = make_float2(v[k].x * fa, v[k].y * fa);
+        A[pad16(2 * i2 + 1)] = make_float2(v[k].z * fb, v[k].w * fb);
     }
     __syncthreads();
-    // Stockham stages: a stage of radix R over sub-length L (the product of the
-    // radices done so far) leaves, in dst, the DFTs of length L*R.
-    int L = 1;
     float2 *src = A, *dst = B;
-    constexpr int stages4 = LOGG / 2, has2 = LOGG & 1;
-#pragma unroll
-    for (int st = 0; st < stages4 + has2; ++st) {
-        const int R = (st < stages4) ? 4 : 2;
-        const int LR = L * R, n = G / LR;
-        // butterflies: G / R of them; butterfly b = (q, k): q in [0, n), k in [0, L)
-        for (int b = threadIdx.x; b < G / R; b += kRowThreads) {
-            const int k = b % L, q = b / L;
-            // Stockham: inputs at stride G / R, outputs at q * L * R + k + r * L
-            float2 x[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-                if (r < R) x[r] = src[b + r * (G / R)];
-            // twiddle for element r: e^{-2 pi i r k / LR} = tw[r k n]
-            if (k > 0) {
-#pragma unroll
-                for (int r = 1; r < 4; ++r)
-                    if (r < R) {
-                        const float2 w = tw[(r * k) * n];
-                        x[r] = cm(x[r], DIR < 0 ? w : conjf2(w));
-                    }
-            }
-            float2 y[4];
-            if (R == 2) {
-                y[0] = make_float2(x[0].x + x[1].x, x[0].y + x[1].y);
-                y[1] = make_float2(x[0].x - x[1].x, x[0].y - x[1].y);
-            } else {
-                // radix-4 DFT with e^{DIR 2 pi i / 4} = DIR * i
-                const float2 s02 = make_float2(x[0].x + x[2].x, x[0].y + x[2].y);
-                const float2 d02 = make_float2(x[0].x - x[2].x, x[0].y - x[2].y);
-                const float2 s13 = make_float2(x[1].x + x[3].x, x[1].y + x[3].y);
-                const float2 d13 = make_float2(x[1].x - x[3].x, x[1].y - x[3].y);
-                // DIR < 0: y1 = d02 - i d13, y3 = d02 + i d13 (signs flipped for DIR > 0)
-                const float sgn = DIR < 0 ? 1.f : -1.f;
-                y[0] = make_float2(s02.x + s13.x, s02.y + s13.y);
-                y[2] = make_float2(s02.x - s13.x, s02.y - s13.y);
-                y[1] = make_float2(d02.x + sgn * d13.y, d02.y - sgn * d13.x);
-                y[3] = make_float2(d02.x - sgn * d13.y, d02.y + sgn * d13.x);
-            }
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-                if (r < R) dst[q * LR + k + r * L] = y[r];
-        }
-        __syncthreads();
-        float2 *tmp = src;
-        src = dst;
-        dst = tmp;
-        L = LR;
-    }
+    stockham_passes<DIR, G, 1>(src, dst, tw_g);
     // post-multiply for the uv -> image direction, store
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
         const int i2 = threadIdx.x + k * kRowThreads;
         if (i2 >= kVec) continue;
-        const float2 a = src[2 * i2], b = src[2 * i2 + 1];
+        const float2 a = src[pad16(2 * i2)], b = src[pad16(2 * i2 + 1)];
         float fa = 1.f, fb = -1.f;
         if (DIR < 0 && corr) {
             fa *= corr[2 * i2];
@@ -146,7 +190,7 @@ __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data,
 
 template <int DIR, int LOGG>
 cudaError_t row_pass(float2 *grid, int64_t rows, const float2 *tw, const float *corr, cudaStream_t st) {
-    const size_t smem = 3 * sizeof(float2) * ((size_t)1 << LOGG);
+    const size_t smem = 2 * sizeof(float2) * (((size_t)1 << LOGG) + ((size_t)1 << LOGG) / 16);
     cudaError_t e = cudaFuncSetAttribute(grid_row_fft_kernel<DIR, LOGG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;

@@ -2,8 +2,10 @@
 
 * Against its definition evaluated in FP64 with numpy (both directions, with
   and without the separable grid correction), relative RMS <= 2e-6.
-* Round trip at 4096^2: image -> uv after uv -> image gives G^2 times the
-  input (a size-independent property of the unnormalised pair).
+* Sizes 64 to 2048 cover every pass sequence of the radix-16 row transform
+  (a last pass of radix 4, 8, none or 2).
+* Round trip at 4096^2 and 8192^2: image -> uv after uv -> image gives G^2
+  times the input (a size-independent property of the unnormalised pair).
 """
 import numpy as np
 import pytest
@@ -27,7 +29,7 @@ def _want(g, c, direction):
     return np.conj(E) @ (cc * g) @ np.conj(E).T
 
 
-@pytest.mark.parametrize("G", [64, 256, 512])
+@pytest.mark.parametrize("G", [64, 128, 256, 512, 2048])
 def test_grid_fft_matches_its_definition(idg, G):
     from idg_gb300 import ops
 
@@ -46,10 +48,10 @@ def test_grid_fft_matches_its_definition(idg, G):
             check_rel(f"grid fft G={G} dir={direction} corr={c is not None}", got, want, TOL)
 
 
-def test_grid_fft_round_trip_4096(idg):
+@pytest.mark.parametrize("G", [4096, 8192])
+def test_grid_fft_round_trip(idg, G):
     from idg_gb300 import ops
 
-    G = 4096
     g = torch.Generator(device="cuda")
     g.manual_seed(3)
     grid = torch.view_as_complex(torch.randn(4 * G * G * 2, generator=g, device="cuda").view(-1, 2)).view(1, 4, G, G)
