@@ -278,7 +278,9 @@ IDG_API int idg_grid_fft(const idg_params *params, void *grid, int direction, co
         return fail(IDG_ERR_UNSUPPORTED, "grid size %d: the grid FFT takes powers of two from 64 to 8192", G);
     if (direction != 1 && direction != -1) return fail(IDG_ERR_INVALID_ARGUMENT, "direction must be +1 or -1");
     if (!grid || !aligned16(grid)) return fail(IDG_ERR_INVALID_ARGUMENT, "grid must be a 16-byte aligned device pointer");
-    cudaError_t e = launch_grid_fft(reinterpret_cast<float2 *>(grid), G, 4 * W, direction, correction,
+    DeviceWords w;
+    if (int rc = device_words(&w)) return rc;
+    cudaError_t e = launch_grid_fft(reinterpret_cast<float2 *>(grid), G, 4 * W, direction, correction, w.status,
                                     reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "grid FFT");
     return IDG_OK;

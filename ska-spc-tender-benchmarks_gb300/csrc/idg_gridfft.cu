@@ -16,8 +16,9 @@
 // by radix-16 Stockham passes in registers (the last one of radix 2, 4 or 8
 // when log2 G is not a multiple of 4), ping-ponging between two shared
 // buffers; twiddles come from a table of
-// e^{-2 pi i m / G} computed in FP64 on the host, read through the read-only
-// cache (one table serves every row of the pass).  All passes are HBM-bound:
+// e^{-2 pi i m / G} computed in FP64 on the host, held per CTA as two
+// 64-entry-scale shared tables whose product gives any entry.  All passes are
+// HBM-bound:
 // 16 bytes per complex cell per pass (read + write).
 #include <cmath>
 #include <map>
@@ -27,6 +28,7 @@
 #include "idg_device.cuh"
 #include "idg_host.h"
 #include "idg_internal.h"
+#include "idg_ptx.cuh"
 
 namespace idg {
 
@@ -34,6 +36,7 @@ namespace {
 
 constexpr int kRowThreads = 256;
 constexpr int kTile = 32;
+constexpr uint64_t kWaitNs = 2000000000ull; // a staged row not complete after 2 s is declared lost
 
 __device__ __forceinline__ float2 cm(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
@@ -94,21 +97,41 @@ __device__ __forceinline__ void dit_stages(float2 (&x)[M]) {
 
 // One Stockham pass of radix R over sub-length L (the product of the radices
 // before it): butterfly b = (q, k), k = b mod L, reads elements b + r G/R,
-// twiddles element r by e^{DIR 2 pi i r k / (L R)} (table e^{-2 pi i m / G},
-// conjugated for DIR = +1), transforms the R values in registers and writes
-// them to q L R + k + r L.
-template <int DIR, int G, int L, int R>
-__device__ __forceinline__ void stockham_pass(const float2 *src, float2 *dst, const float2 *tw_g) {
+// twiddles element r by e^{DIR 2 pi i r k / (L R)} (e^{-2 pi i m / G} from the
+// two shared tables at tw_g, conjugated for DIR = +1), transforms the R
+// values in registers and writes them to q L R + k + r L.
+// FIRST: src is the row as copied from global memory (unpadded), and each
+// element i is multiplied on the way in by (-1)^i (and by corr[i] for the
+// image -> uv direction).
+// Twiddle e^{-2 pi i m / G}, m < G, from two shared tables built once per
+// CTA: lo[j] = e^{-2 pi i j / G} (j < 64) and hi[j] = e^{-2 pi i 64 j / G}.
+__device__ __forceinline__ float2 twiddle(const float2 *lo, const float2 *hi, int m) {
+    return cm(lo[m & 63], hi[m >> 6]);
+}
+
+template <int DIR, int G, int L, int R, bool FIRST = false>
+__device__ __forceinline__ void stockham_pass(const float2 *src, float2 *dst, const float2 *tw_g,
+                                              const float *corr = nullptr) {
     constexpr int n = G / (L * R);
     for (int b = threadIdx.x; b < G / R; b += kRowThreads) {
         const int k = b % L, q = b / L;
         float2 x[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) x[r] = src[pad16(b + r * (G / R))];
+        for (int r = 0; r < R; ++r) {
+            if (FIRST) {
+                const int i = b + r * (G / R);
+                float f = (i & 1) ? -1.f : 1.f;
+                if (DIR > 0 && corr) f *= __ldg(corr + i);
+                const float2 e = src[i];
+                x[r] = make_float2(e.x * f, e.y * f);
+            } else {
+                x[r] = src[pad16(b + r * (G / R))];
+            }
+        }
         if (L > 1 && k > 0) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
-                const float2 w = __ldg(tw_g + (r * k) * n);
+                const float2 w = twiddle(tw_g, tw_g + 64, (r * k) * n);
                 x[r] = cm(x[r], DIR < 0 ? w : conjf2(w));
             }
         }
@@ -135,80 +158,112 @@ __device__ __forceinline__ void stockham_passes(float2 *&src, float2 *&dst, cons
     }
 }
 
-// One FFT over the CTA's row (length G = 2^LOGG, row stride G).  DIR = -1
-// uses e^{-2 pi i ...}, DIR = +1 its conjugate.  Element i of the row is
+// Row FFTs (length G = 2^LOGG, row stride G) by persistent CTAs.  DIR = -1
+// uses e^{-2 pi i ...}, DIR = +1 its conjugate.  Element i of a row is
 // multiplied by (-1)^i before and after the transform (the centre shifts of
 // this dimension), and by corr[i] (when given) after it for DIR = -1 or before
-// it for DIR = +1.  The row is staged in padded shared memory with all of a
-// thread's 16-byte loads issued before any is used, then transformed by
-// radix-16 Stockham passes in registers (three for G = 4096).
+// it for DIR = +1.  Each CTA takes rows blockIdx.x, + gridDim.x, ...: a row
+// arrives in a staging buffer by one bulk async copy (completion counted on an
+// mbarrier, waits bounded by kWaitNs), the first radix-16 pass reads it from
+// there (pre-multiplication folded in) into a padded buffer, and the next
+// row's copy is issued as soon as the staging buffer is free, so it overlaps
+// the remaining passes and the store of the current row.  A copy that does not
+// arrive in time sets the timeout bit of `status` and the CTA stops.
 template <int DIR, int LOGG>
-__global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data, const float2 *tw_g,
-                                                                   const float *corr) {
+__global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data, int64_t rows, const float2 *tw_g,
+                                                                   const float *corr, unsigned *status) {
     constexpr int G = 1 << LOGG, kVec = G / 2;  // float4 per row
     constexpr int kPer = (kVec + kRowThreads - 1) / kRowThreads;
-    extern __shared__ float2 sm[];
-    float2 *A = sm, *B = sm + (G + G / 16);
-    const int row = blockIdx.x;
-    float2 *p = data + (int64_t)row * G;
-    float4 v[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-        const int i2 = threadIdx.x + k * kRowThreads;
-        if (i2 < kVec) v[k] = reinterpret_cast<const float4 *>(p)[i2];
+    constexpr int R1 = G >= 16 ? 16 : G;
+    constexpr uint32_t kRowBytes = (uint32_t)G * 8u;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    float2 *C = reinterpret_cast<float2 *>(smem + 16); // staged row (bulk-copy target)
+    float2 *A = C + G, *B = A + (G + G / 16);          // padded ping-pong buffers
+    __shared__ float2 tws[64 + G / 64];                 // twiddle tables (see twiddle())
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_init_fence();
+        abort_flag = 0;
     }
-    // pre-multiply for the image -> uv direction
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-        const int i2 = threadIdx.x + k * kRowThreads;
-        if (i2 >= kVec) continue;
-        float fa = 1.f, fb = -1.f; // (-1)^i for i = 2 i2, 2 i2 + 1
-        if (DIR > 0 && corr) {
-            fa *= corr[2 * i2];
-            fb *= corr[2 * i2 + 1];
-        }
-        A[pad16(2 * i2)] = make_float2(v[k].x * fa, v[k].y * fa);
-        A[pad16(2 * i2 + 1)] = make_float2(v[k].z * fb, v[k].w * fb);
-    }
+    for (int j = tid; j < 64 + G / 64; j += kRowThreads) tws[j] = tw_g[j < 64 ? j : 64 * (j - 64)];
     __syncthreads();
-    float2 *src = A, *dst = B;
-    stockham_passes<DIR, G, 1>(src, dst, tw_g);
-    // post-multiply for the uv -> image direction, store
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-        const int i2 = threadIdx.x + k * kRowThreads;
-        if (i2 >= kVec) continue;
-        const float2 a = src[pad16(2 * i2)], b = src[pad16(2 * i2 + 1)];
-        float fa = 1.f, fb = -1.f;
-        if (DIR < 0 && corr) {
-            fa *= corr[2 * i2];
-            fb *= corr[2 * i2 + 1];
+    uint32_t phase = 0;
+    int64_t row = blockIdx.x;
+    if (tid == 0 && row < rows) {
+        mbar_arrive_expect_tx(bar, kRowBytes);
+        bulk_g2s(C, data + row * G, kRowBytes, bar);
+    }
+    for (; row < rows; row += gridDim.x) {
+        if (!mbar_wait_bounded(bar, phase, kWaitNs)) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) {
+            if (tid == 0) {
+                flag_status(status, kStatusTimeout);
+                mbar_wait_bounded(bar, phase, kWaitNs); // the copy in flight, once more
+            }
+            break;
         }
-        reinterpret_cast<float4 *>(p)[i2] = make_float4(a.x * fa, a.y * fa, b.x * fb, b.y * fb);
+        phase ^= 1u;
+        stockham_pass<DIR, G, 1, R1, true>(C, B, tws, corr);
+        __syncthreads(); // C read by every thread: free for the next row
+        if (tid == 0 && row + gridDim.x < rows) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(bar, kRowBytes);
+            bulk_g2s(C, data + (row + gridDim.x) * G, kRowBytes, bar);
+        }
+        float2 *src = B, *dst = A;
+        stockham_passes<DIR, G, R1>(src, dst, tws);
+        // post-multiply for the uv -> image direction, store
+        float2 *p = data + row * G;
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int i2 = tid + k * kRowThreads;
+            if (i2 >= kVec) continue;
+            const float2 a = src[pad16(2 * i2)], b = src[pad16(2 * i2 + 1)];
+            float fa = 1.f, fb = -1.f;
+            if (DIR < 0 && corr) {
+                fa *= corr[2 * i2];
+                fb *= corr[2 * i2 + 1];
+            }
+            reinterpret_cast<float4 *>(p)[i2] = make_float4(a.x * fa, a.y * fa, b.x * fb, b.y * fb);
+        }
+        __syncthreads(); // the output buffer is read before the next row's first pass writes B
     }
 }
 
 template <int DIR, int LOGG>
-cudaError_t row_pass(float2 *grid, int64_t rows, const float2 *tw, const float *corr, cudaStream_t st) {
-    const size_t smem = 2 * sizeof(float2) * (((size_t)1 << LOGG) + ((size_t)1 << LOGG) / 16);
-    cudaError_t e = cudaFuncSetAttribute(grid_row_fft_kernel<DIR, LOGG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+cudaError_t row_pass(float2 *grid, int64_t rows, const float2 *tw, const float *corr, unsigned *status,
+                     cudaStream_t st) {
+    constexpr size_t G = (size_t)1 << LOGG;
+    const size_t smem = 16 + sizeof(float2) * (G + 2 * (G + G / 16));
+    auto kern = grid_row_fft_kernel<DIR, LOGG>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    grid_row_fft_kernel<DIR, LOGG><<<(unsigned)rows, kRowThreads, smem, st>>>(grid, tw, corr);
+    int per_sm = 0, dev = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRowThreads, smem)) != cudaSuccess) return e;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (blocks > rows) blocks = rows;
+    kern<<<(unsigned)blocks, kRowThreads, smem, st>>>(grid, rows, tw, corr, status);
     return cudaGetLastError();
 }
 
 template <int DIR>
-cudaError_t row_pass_g(int logG, float2 *grid, int64_t rows, const float2 *tw, const float *corr, cudaStream_t st) {
+cudaError_t row_pass_g(int logG, float2 *grid, int64_t rows, const float2 *tw, const float *corr, unsigned *status,
+                       cudaStream_t st) {
     switch (logG) {
-    case 6: return row_pass<DIR, 6>(grid, rows, tw, corr, st);
-    case 7: return row_pass<DIR, 7>(grid, rows, tw, corr, st);
-    case 8: return row_pass<DIR, 8>(grid, rows, tw, corr, st);
-    case 9: return row_pass<DIR, 9>(grid, rows, tw, corr, st);
-    case 10: return row_pass<DIR, 10>(grid, rows, tw, corr, st);
-    case 11: return row_pass<DIR, 11>(grid, rows, tw, corr, st);
-    case 12: return row_pass<DIR, 12>(grid, rows, tw, corr, st);
-    case 13: return row_pass<DIR, 13>(grid, rows, tw, corr, st);
+    case 6: return row_pass<DIR, 6>(grid, rows, tw, corr, status, st);
+    case 7: return row_pass<DIR, 7>(grid, rows, tw, corr, status, st);
+    case 8: return row_pass<DIR, 8>(grid, rows, tw, corr, status, st);
+    case 9: return row_pass<DIR, 9>(grid, rows, tw, corr, status, st);
+    case 10: return row_pass<DIR, 10>(grid, rows, tw, corr, status, st);
+    case 11: return row_pass<DIR, 11>(grid, rows, tw, corr, status, st);
+    case 12: return row_pass<DIR, 12>(grid, rows, tw, corr, status, st);
+    case 13: return row_pass<DIR, 13>(grid, rows, tw, corr, status, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -267,7 +322,8 @@ cudaError_t twiddles(int G, const float2 **out) {
 
 bool grid_fft_size_supported(int G) { return G >= 64 && G <= 8192 && (G & (G - 1)) == 0; }
 
-cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, const float *corr, cudaStream_t st) {
+cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, const float *corr, unsigned *status,
+                            cudaStream_t st) {
     if (!grid_fft_size_supported(G)) return cudaErrorInvalidValue;
     const float2 *tw = nullptr;
     cudaError_t e = twiddles(G, &tw);
@@ -276,8 +332,8 @@ cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, cons
     while ((1 << logG) < G) ++logG;
     const int64_t rows = (int64_t)planes * G;
     auto rowpass = [&]() -> cudaError_t {
-        return direction < 0 ? row_pass_g<-1>(logG, grid, rows, tw, corr, st)
-                             : row_pass_g<1>(logG, grid, rows, tw, corr, st);
+        return direction < 0 ? row_pass_g<-1>(logG, grid, rows, tw, corr, status, st)
+                             : row_pass_g<1>(logG, grid, rows, tw, corr, status, st);
     };
     const dim3 tgrid(G / kTile, G / kTile, planes);
     // rows (x), transpose, rows (y), transpose back
