@@ -75,6 +75,10 @@ typedef struct idg_subgrid_ext {
 #define IDG_FLAG_DEGRID_ATERM_REFCPU 0x1u /* degridder applies A1^H P A2 (degridding_benchmark.cpp:113)
                                              instead of the adjoint A1 P A2^H (degridding_benchmark.cu:56) */
 #define IDG_FLAG_NO_TAPER 0x2u            /* gridder/degridder skip the spheroidal (the FFT applies it) */
+#define IDG_FLAG_TEST_LOST_COPY 0x100u    /* tests only: the batched gridders and the grid FFT declare their
+                                             first staged copy 16 bytes larger than what they copy, so its
+                                             bounded wait (2 s) runs out: the kernel sets status bit 2 and
+                                             stops, without faulting the GPU (see idg_device_status) */
 
 /* Geometry and physics shared by all kernels of one call. */
 typedef struct idg_params {
@@ -111,7 +115,9 @@ IDG_API int idg_abi_version(void);
 IDG_API const char *idg_last_error(void);
 /* Reads and (if clear != 0) resets the device-side check word of the current
  * device: bit 0 = a plan entry named rows/stations/A-terms out of range,
- * bit 1 = a shape the kernel cannot handle.  Synchronises `stream`. */
+ * bit 1 = a shape the kernel cannot handle, bit 2 = a staged copy did not
+ * arrive within its time limit (the kernel stopped; its outputs are
+ * incomplete).  Synchronises `stream`. */
 IDG_API int idg_device_status(void *stream, uint32_t *status, int clear);
 
 /* ------------------------------------------------------------------ */

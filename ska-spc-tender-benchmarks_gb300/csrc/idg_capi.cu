@@ -281,6 +281,7 @@ IDG_API int idg_grid_fft(const idg_params *params, void *grid, int direction, co
     DeviceWords w;
     if (int rc = device_words(&w)) return rc;
     cudaError_t e = launch_grid_fft(reinterpret_cast<float2 *>(grid), G, 4 * W, direction, correction, w.status,
+                                    (params->flags & IDG_FLAG_TEST_LOST_COPY) != 0,
                                     reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "grid FFT");
     return IDG_OK;

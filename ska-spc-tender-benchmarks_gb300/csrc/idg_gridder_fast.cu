@@ -343,8 +343,10 @@ __device__ __forceinline__ bool stage_tile(const KernelArgs &a, const SubgridInf
     __syncthreads(); // previous tile fully consumed (raw, expanded operands, coef)
     if (tid == 0) {
         const uint32_t row_bytes = (uint32_t)ncc * 32u;
+        // IDG_FLAG_TEST_LOST_COPY: expect 16 bytes that never come, so that the wait runs out
+        const uint32_t lost = (a.flags & IDG_FLAG_TEST_LOST_COPY) ? 16u : 0u;
         fence_proxy_async();
-        mbar_arrive_expect_tx(&head->bar, row_bytes * (uint32_t)tt);
+        mbar_arrive_expect_tx(&head->bar, row_bytes * (uint32_t)tt + lost);
         const float4 *src = a.vis + ((int64_t)si.row0 + t0) * a.C * 2 + (int64_t)(si.c0 + cb) * 2;
         for (int r = 0; r < tt; ++r)
             bulk_g2s(raw + (size_t)r * ncc * 2, src + (int64_t)r * a.C * 2, row_bytes, &head->bar);

@@ -168,10 +168,12 @@ __device__ __forceinline__ void stockham_passes(float2 *&src, float2 *&dst, cons
 // there (pre-multiplication folded in) into a padded buffer, and the next
 // row's copy is issued as soon as the staging buffer is free, so it overlaps
 // the remaining passes and the store of the current row.  A copy that does not
-// arrive in time sets the timeout bit of `status` and the CTA stops.
+// arrive in time sets the timeout bit of `status` and the CTA stops (`lost`
+// extra expected bytes on the first copy make that happen in tests).
 template <int DIR, int LOGG>
 __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data, int64_t rows, const float2 *tw_g,
-                                                                   const float *corr, unsigned *status) {
+                                                                   const float *corr, unsigned *status,
+                                                                   uint32_t lost) {
     constexpr int G = 1 << LOGG, kVec = G / 2;  // float4 per row
     constexpr int kPer = (kVec + kRowThreads - 1) / kRowThreads;
     constexpr int R1 = G >= 16 ? 16 : G;
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data,
     uint32_t phase = 0;
     int64_t row = blockIdx.x;
     if (tid == 0 && row < rows) {
-        mbar_arrive_expect_tx(bar, kRowBytes);
+        mbar_arrive_expect_tx(bar, kRowBytes + lost); // lost > 0 only under IDG_FLAG_TEST_LOST_COPY
         bulk_g2s(C, data + row * G, kRowBytes, bar);
     }
     for (; row < rows; row += gridDim.x) {
@@ -236,7 +238,7 @@ __global__ void __launch_bounds__(kRowThreads) grid_row_fft_kernel(float2 *data,
 
 template <int DIR, int LOGG>
 cudaError_t row_pass(float2 *grid, int64_t rows, const float2 *tw, const float *corr, unsigned *status,
-                     cudaStream_t st) {
+                     uint32_t lost, cudaStream_t st) {
     constexpr size_t G = (size_t)1 << LOGG;
     const size_t smem = 16 + sizeof(float2) * (G + 2 * (G + G / 16));
     auto kern = grid_row_fft_kernel<DIR, LOGG>;
@@ -248,22 +250,22 @@ cudaError_t row_pass(float2 *grid, int64_t rows, const float2 *tw, const float *
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
     if (blocks > rows) blocks = rows;
-    kern<<<(unsigned)blocks, kRowThreads, smem, st>>>(grid, rows, tw, corr, status);
+    kern<<<(unsigned)blocks, kRowThreads, smem, st>>>(grid, rows, tw, corr, status, lost);
     return cudaGetLastError();
 }
 
 template <int DIR>
 cudaError_t row_pass_g(int logG, float2 *grid, int64_t rows, const float2 *tw, const float *corr, unsigned *status,
-                       cudaStream_t st) {
+                       uint32_t lost, cudaStream_t st) {
     switch (logG) {
-    case 6: return row_pass<DIR, 6>(grid, rows, tw, corr, status, st);
-    case 7: return row_pass<DIR, 7>(grid, rows, tw, corr, status, st);
-    case 8: return row_pass<DIR, 8>(grid, rows, tw, corr, status, st);
-    case 9: return row_pass<DIR, 9>(grid, rows, tw, corr, status, st);
-    case 10: return row_pass<DIR, 10>(grid, rows, tw, corr, status, st);
-    case 11: return row_pass<DIR, 11>(grid, rows, tw, corr, status, st);
-    case 12: return row_pass<DIR, 12>(grid, rows, tw, corr, status, st);
-    case 13: return row_pass<DIR, 13>(grid, rows, tw, corr, status, st);
+    case 6: return row_pass<DIR, 6>(grid, rows, tw, corr, status, lost, st);
+    case 7: return row_pass<DIR, 7>(grid, rows, tw, corr, status, lost, st);
+    case 8: return row_pass<DIR, 8>(grid, rows, tw, corr, status, lost, st);
+    case 9: return row_pass<DIR, 9>(grid, rows, tw, corr, status, lost, st);
+    case 10: return row_pass<DIR, 10>(grid, rows, tw, corr, status, lost, st);
+    case 11: return row_pass<DIR, 11>(grid, rows, tw, corr, status, lost, st);
+    case 12: return row_pass<DIR, 12>(grid, rows, tw, corr, status, lost, st);
+    case 13: return row_pass<DIR, 13>(grid, rows, tw, corr, status, lost, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -323,7 +325,8 @@ cudaError_t twiddles(int G, const float2 **out) {
 bool grid_fft_size_supported(int G) { return G >= 64 && G <= 8192 && (G & (G - 1)) == 0; }
 
 cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, const float *corr, unsigned *status,
-                            cudaStream_t st) {
+                            bool test_lost_copy, cudaStream_t st) {
+    const uint32_t lost = test_lost_copy ? 16u : 0u;
     if (!grid_fft_size_supported(G)) return cudaErrorInvalidValue;
     const float2 *tw = nullptr;
     cudaError_t e = twiddles(G, &tw);
@@ -332,8 +335,8 @@ cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, cons
     while ((1 << logG) < G) ++logG;
     const int64_t rows = (int64_t)planes * G;
     auto rowpass = [&]() -> cudaError_t {
-        return direction < 0 ? row_pass_g<-1>(logG, grid, rows, tw, corr, status, st)
-                             : row_pass_g<1>(logG, grid, rows, tw, corr, status, st);
+        return direction < 0 ? row_pass_g<-1>(logG, grid, rows, tw, corr, status, lost, st)
+                             : row_pass_g<1>(logG, grid, rows, tw, corr, status, lost, st);
     };
     const dim3 tgrid(G / kTile, G / kTile, planes);
     // rows (x), transpose, rows (y), transpose back

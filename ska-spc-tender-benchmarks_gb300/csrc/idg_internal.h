@@ -32,7 +32,7 @@ cudaError_t launch_subgrid_fft(float2 *data, int64_t nr_subgrids, int S, int dir
 
 bool grid_fft_size_supported(int G);
 cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, const float *correction,
-                            unsigned *status, cudaStream_t stream);
+                            unsigned *status, bool test_lost_copy, cudaStream_t stream);
 
 cudaError_t launch_adder(const struct idg_metadata *md, int64_t nr_subgrids, int S, int G, int W,
                          const float2 *subgrids, float2 *grid, cudaStream_t stream);

@@ -26,6 +26,7 @@ IDG_ERR_REJECTED = 8
 
 IDG_FLAG_DEGRID_ATERM_REFCPU = 0x1
 IDG_FLAG_NO_TAPER = 0x2
+IDG_FLAG_TEST_LOST_COPY = 0x100
 
 VARIANT_PLAIN = 0
 VARIANT_BATCHED = 1
