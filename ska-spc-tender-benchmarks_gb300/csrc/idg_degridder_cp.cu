@@ -18,6 +18,9 @@
 // of a group each sum a quarter of the staged pixels; their partial sums are
 // combined with two levels of 64-bit warp shuffles and each lane writes CB/4
 // channels.
+// The mirror-quad degridder (degridder_quad_kernel, below) keeps this work
+// split and channel packing but stages quads of pixels (+-hx, +-hy) instead of
+// pixels: its MACs share each quad's phase factors (see its section).
 #include "idg_device.cuh"
 #include "idg_internal.h"
 #include "idg_ptx.cuh"
