@@ -25,6 +25,21 @@ def test_header_and_binding_agree(idg):
     assert set(declared_symbols()) == set(_lib.exported_symbols())
 
 
+def test_header_constants_match_the_binding(idg):
+    """Every status code, flag, variant and job kind of the header has the same
+    value in the Python binding (IDG_VARIANT_* are VARIANT_* there)."""
+    from idg_gb300 import _lib
+
+    text = open(HEADER).read()
+    consts = {m[0]: int(m[1], 0) for m in re.findall(r"#define\s+(IDG_(?:FLAG|VARIANT|JOB)_\w+)\s+(0x[0-9a-fA-F]+|\d+)u?",
+                                                     text)}
+    consts.update({m[0]: int(m[1]) for m in re.findall(r"\b(IDG_(?:OK|ERR_\w+))\s*=\s*(\d+)", text)})
+    assert len(consts) >= 15
+    for name, value in consts.items():
+        py = name.replace("IDG_VARIANT_", "VARIANT_")
+        assert getattr(_lib, py) == value, name
+
+
 def test_library_exports_every_declared_symbol(idg):
     lib = idg.load()
     for name in declared_symbols():
