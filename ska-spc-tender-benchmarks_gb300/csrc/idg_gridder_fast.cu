@@ -600,10 +600,12 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 // ---------------------------------------------------------------------------
 // SHP: every quad of the thread has the same x column (NT a multiple of S/2),
 // so P is one sincos per thread, shared by all its quads.
-template <int GP, bool FAST, int UNR, bool SHP>
-__device__ __forceinline__ void quad_tile(f2 (&acc)[GP][4][8], const f2 (&hx)[GP], const f2 (&hy)[GP],
-                                          const f2 (&nn)[GP], const float4 *coef, const float4 *vq, const f2 *kp,
-                                          int tt, int ncc) {
+// qg: the thread's quad geometry in shared memory, qg[(3 j + c) * NT] for
+// quad pair j and c = hx, hy, n (read once per timestep, not held in registers
+// across the channel loop).
+template <int GP, bool FAST, int UNR, bool SHP, int NT>
+__device__ __forceinline__ void quad_tile(f2 (&acc)[GP][4][8], const f2 *qg, const float4 *coef, const float4 *vq,
+                                          const f2 *kp, int tt, int ncc) {
     for (int t = 0; t < tt; ++t) {
         const float4 c0 = coef[3 * t], c1 = coef[3 * t + 1], c2 = coef[3 * t + 2];
         const f2 A2 = pack2(c0.x, c0.y), B2 = pack2(c0.z, c0.w), G2 = pack2(c1.x, c1.y);
@@ -611,12 +613,13 @@ __device__ __forceinline__ void quad_tile(f2 (&acc)[GP][4][8], const f2 (&hx)[GP
         f2 tx[GP], ty[GP], tn[GP], qx[GP], qy[GP], qn[GP];
 #pragma unroll
         for (int j = 0; j < GP; ++j) {
-            tx[j] = reduce_2pi(fmul2(A2, hx[j]));
-            ty[j] = reduce_2pi(fmul2(B2, hy[j]));
-            tn[j] = reduce_2pi(fmul2(G2, nn[j]));
-            qx[j] = fmul2(QU, hx[j]);
-            qy[j] = fmul2(QV, hy[j]);
-            qn[j] = fmul2(QW, nn[j]);
+            const f2 hx = qg[(3 * j) * NT], hy = qg[(3 * j + 1) * NT], nn = qg[(3 * j + 2) * NT];
+            tx[j] = reduce_2pi(fmul2(A2, hx));
+            ty[j] = reduce_2pi(fmul2(B2, hy));
+            tn[j] = reduce_2pi(fmul2(G2, nn));
+            qx[j] = fmul2(QU, hx);
+            qy[j] = fmul2(QV, hy);
+            qn[j] = fmul2(QW, nn);
         }
         const float4 *vt = vq + (size_t)t * ncc * 4;
 #pragma unroll UNR
@@ -752,7 +755,7 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
             // the quads of this thread: pair j holds quads g0 (low half) and g1 (high half);
             // each quad is named by its pixel (gx, gy) in the low-x, low-y quadrant
             int qd[GP][2];
-            f2 hx[GP], hy[GP], nn[GP];
+            f2 *qg = reinterpret_cast<f2 *>(smem + L.total) + tid;
 #pragma unroll
             for (int j = 0; j < GP; ++j) {
                 float gxh[2], gyh[2], gnn[2];
@@ -767,9 +770,9 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
                     gyh[h] = geo.y;
                     gnn[h] = geo.z;
                 }
-                hx[j] = pack2(gxh[0], gxh[1]);
-                hy[j] = pack2(gyh[0], gyh[1]);
-                nn[j] = pack2(gnn[0], gnn[1]);
+                qg[(3 * j) * kT] = pack2(gxh[0], gxh[1]);
+                qg[(3 * j + 1) * kT] = pack2(gyh[0], gyh[1]);
+                qg[(3 * j + 2) * kT] = pack2(gnn[0], gnn[1]);
             }
 
             for (int cb = 0; cb < nc; cb += chunk) {
@@ -795,13 +798,13 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
                     __syncthreads();
                     if (shared_x) {
                         if (head->fast)
-                            quad_tile<GP, true, UNR, true>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                            quad_tile<GP, true, UNR, true, kT>(acc, qg, coef, vq, kap + cb, tt, ncc);
                         else
-                            quad_tile<GP, false, UNR, true>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                            quad_tile<GP, false, UNR, true, kT>(acc, qg, coef, vq, kap + cb, tt, ncc);
                     } else if (head->fast) {
-                        quad_tile<GP, true, UNR, false>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                        quad_tile<GP, true, UNR, false, kT>(acc, qg, coef, vq, kap + cb, tt, ncc);
                     } else {
-                        quad_tile<GP, false, UNR, false>(acc, hx, hy, nn, coef, vq, kap + cb, tt, ncc);
+                        quad_tile<GP, false, UNR, false, kT>(acc, qg, coef, vq, kap + cb, tt, ncc);
                     }
                 }
                 if (head->abort) break;
@@ -905,7 +908,7 @@ template <int NT, int GP, int TV, int MINB, int UNR>
 cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
     if (a.S % 2 != 0) return cudaErrorInvalidValue;
     auto kern = gridder_quad_kernel<NT, GP, TV, MINB, UNR>;
-    const size_t smem = layout(a.S, a.C, TV).total;
+    const size_t smem = layout(a.S, a.C, TV).total + (size_t)NT * GP * 3 * sizeof(f2); // + quad geometry
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
