@@ -364,7 +364,7 @@ cudaError_t launch_cp(const KernelArgs &a, cudaStream_t stream) {
 }
 
 // ---------------------------------------------------------------------------
-// Mirror-quad form of the degridder (shapes 13-16 of this family).  A quad is
+// Mirror-quad form of the degridder (shapes 13-17 of this family).  A quad is
 // the four pixels (hx, hy), (-hx, -hy), (-hx, hy), (hx, -hy) of one n; with the
 // gridder's factors P = e^{i a_c hx}, Q = e^{i b_c hy}, R = e^{i g_c n},
 // X = P Q and Y = conj(P) Q, the four pixels' phasors are conj of X R,
@@ -444,7 +444,81 @@ __device__ __forceinline__ void quad_macs(f2 (&acc)[NPAIR][4][2], const KP &kp, 
     }
 }
 
-template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false>
+// Column form (COL): quads are staged column by column (slot i of a batch is
+// quad qb + i in column-major order), so the slots a lane visits (i, i + 4, ...)
+// run down one column for Sh / 4 steps when Sh is a multiple of 4.  P depends
+// on hx only: a lane computes it when its quad's hx changes and keeps it
+// (Pc, Ps per channel pair, 16 registers) for the next quads, which leaves two
+// sincos per quad and channel (Q and R) plus P once per column run.  The MACs
+// are those of quad_macs.  The extra registers need the uncapped budget of
+// 8 warps per SM; at 12 warps the spills cost more than the saved sincos.
+template <int NPAIR, bool FAST, typename KP>
+__device__ __forceinline__ void column_factors(f2 (&Pc)[NPAIR], f2 (&Ps)[NPAIR], const KP &kp, float hx, float A,
+                                               float qu) {
+    const float tx = reduce_2pi_s(A * hx), qx = qu * hx;
+    const f2 TX = pack2(tx, tx), QX = pack2(qx, qx);
+#pragma unroll
+    for (int j = 0; j < NPAIR; ++j) {
+        f2 ap = ffma2(kappa_pair(kp, j), QX, TX);
+        if (!FAST) ap = reduce_2pi(ap);
+        sincos_pair(ap, Pc[j], Ps[j]);
+    }
+}
+
+template <int NPAIR, bool FAST, typename KP>
+__device__ __forceinline__ void quad_macs_col(f2 (&acc)[NPAIR][4][2], const f2 (&Pc)[NPAIR], const f2 (&Ps)[NPAIR],
+                                              const KP &kp, float4 g, float B, float Gc, float qv, float qw,
+                                              uint32_t ops_addr) {
+    const float ty = reduce_2pi_s(B * g.y), tn = reduce_2pi_s(Gc * g.z);
+    const f2 TY = pack2(ty, ty), TN = pack2(tn, tn);
+    const float qy = qv * g.y, qn = qw * g.z;
+    const f2 QY = pack2(qy, qy), QN = pack2(qn, qn);
+    f2 o[32];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) lds2(ops_addr + 16 * q, o[2 * q], o[2 * q + 1]);
+#pragma unroll
+    for (int j = 0; j < NPAIR; ++j) {
+        const f2 kj = kappa_pair(kp, j);
+        f2 aq = ffma2(kj, QY, TY), ar = ffma2(kj, QN, TN);
+        if (!FAST) {
+            aq = reduce_2pi(aq);
+            ar = reduce_2pi(ar);
+        }
+        f2 Qc, Qs, Rc, Rs;
+        sincos_pair(aq, Qc, Qs);
+        sincos_pair(ar, Rc, Rs);
+        const f2 nPs = neg2(Ps[j]), nRs = neg2(Rs);
+        const f2 m1 = fmul2(Pc[j], Qc), m3 = fmul2(Pc[j], Qs);
+        const f2 Xr = ffma2(nPs, Qs, m1), Yr = ffma2(Ps[j], Qs, m1);
+        const f2 Xi = ffma2(Ps[j], Qc, m3), Yi = ffma2(nPs, Qc, m3);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const f2 *p = o + 8 * k;
+            const f2 Zr = ffma2(Yi, p[3], ffma2(Yr, p[2], ffma2(Xi, p[1], fmul2(Xr, p[0]))));
+            const f2 Zi = ffma2(Yi, p[7], ffma2(Yr, p[6], ffma2(Xi, p[5], fmul2(Xr, p[4]))));
+            acc[j][k][0] = ffma2(Rs, Zi, ffma2(Rc, Zr, acc[j][k][0]));
+            acc[j][k][1] = ffma2(nRs, Zr, ffma2(Rc, Zi, acc[j][k][1]));
+        }
+    }
+}
+
+template <int NPAIR, bool FAST, typename KP>
+__device__ __forceinline__ void column_loop(f2 (&acc)[NPAIR][4][2], const KP &kp, const float4 *geo, float4 c0,
+                                            float4 c1, uint32_t ops_addr, int part, int nq) {
+    f2 Pc[NPAIR], Ps[NPAIR];
+    float cur = __int_as_float(0x7fc00000); // NaN: the first quad always computes P
+    for (int i = part; i < nq; i += kLanes) {
+        const float4 g = geo[i];
+        if (!(g.x == cur)) {
+            cur = g.x;
+            column_factors<NPAIR, FAST>(Pc, Ps, kp, g.x, c0.x, c0.w);
+        }
+        quad_macs_col<NPAIR, FAST>(acc, Pc, Ps, kp, g, c0.y, c0.z, c1.x, c1.y, ops_addr + kQuadStride * (uint32_t)i);
+    }
+}
+
+// COL: the column form (column_loop); otherwise quads row by row.
+template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false, bool COL = false>
 __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) {
     constexpr int kT = NT, kCB = CB, kNP = CB / 2;
     static_assert(CB == 4 || CB == 8, "channel groups of 4 or 8");
@@ -502,7 +576,8 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
             __syncthreads(); // previous batch consumed
             // ---- stage the batch's quads: A-terms and taper applied, sums and differences
             for (int i = tid; i < nq; i += kT) {
-                const int g = qb + i, gy = g / Sh, gx = g - gy * Sh;
+                const int g = qb + i;
+                const int gy = COL ? g % Sh : g / Sh, gx = COL ? g / Sh : g % Sh;
                 // 0 = (gx, gy), 1 = (S-1-gx, S-1-gy), 2 = (S-1-gx, gy), 3 = (gx, S-1-gy)
                 const int qx[4] = {gx, S - 1 - gx, S - 1 - gx, gx};
                 const int qy[4] = {gy, S - 1 - gy, gy, S - 1 - gy};
@@ -557,7 +632,12 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
 #pragma unroll
                         for (int k = 0; k < 4; ++k) acc[j][k][0] = acc[j][k][1] = 0ull;
                     const float *kps = kap + cfirst;
-                    if (fast) {
+                    if (COL) {
+                        if (fast)
+                            column_loop<kNP, true>(acc, kps, geo, c0, c1, ops_addr, part, nq);
+                        else
+                            column_loop<kNP, false>(acc, kps, geo, c0, c1, ops_addr, part, nq);
+                    } else if (fast) {
 #pragma unroll UNR
                         for (int i = part; i < nq; i += kLanes) {
                             if (KSM)
@@ -598,10 +678,10 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
     }
 }
 
-template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false>
+template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false, bool COL = false>
 cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
     if (a.S % 2 != 0) return cudaErrorInvalidValue;
-    auto kern = degridder_quad_kernel<NT, QB, MINB, CB, UNR, KSM>;
+    auto kern = degridder_quad_kernel<NT, QB, MINB, CB, UNR, KSM, COL>;
     const size_t smem = quad_layout(a.S, a.C, QB).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -621,7 +701,7 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int degridder_cp_shapes() { return 17; }
+int degridder_cp_shapes() { return 18; }
 
 // Channel-pair shapes (index within this family):
 //   0: 128 threads, 8-channel groups, 256-pixel batches, 4 CTAs/SM (16 warps)
@@ -641,12 +721,14 @@ int degridder_cp_shapes() { return 17; }
 //  14: mirror quads, 128 threads, 8-channel groups, 256-quad batches, 3 CTAs/SM (12 warps)
 //  15: shape 13 with the quad loop unrolled by two
 //  16: shape 14 reading each channel pair's kappa from shared memory when used
+//  17: mirror quads in column form (P kept per column run), 2 CTAs/SM
 cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
     case 13: return launch_quad<128, 256, 2, 8, 1>(a, stream);
     case 14: return launch_quad<128, 256, 3, 8, 1>(a, stream);
     case 15: return launch_quad<128, 256, 2, 8, 2>(a, stream);
     case 16: return launch_quad<128, 256, 3, 8, 1, true>(a, stream);
+    case 17: return launch_quad<128, 256, 2, 8, 1, true, true>(a, stream);
     case 1: return launch_cp<128, 512, 3, 8, 0, 2>(a, stream);
     case 2: return launch_cp<128, 512, 2, 16, 0, 1>(a, stream);
     case 3: return launch_cp<128, 512, 3, 8, kGaussCp, 1>(a, stream);
