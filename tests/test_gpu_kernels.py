@@ -316,11 +316,13 @@ def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
     tuning.set_shapes(S, *saved)
 
 
-@pytest.mark.parametrize("S", [8, 16, 24, 48, 64])
+@pytest.mark.parametrize("S", [8, 16, 20, 24, 36, 48, 64])
 def test_every_batched_shape_at_other_subgrid_sizes(oracle_mod, idg, S):
     """Every launch shape of both batched kernels (pixel-pair and channel-pair
     degridders included) on an uneven plan with subgrid sizes that need partial
-    pixel passes and channel ranges that are not multiples of the channel group."""
+    pixel passes and channel ranges that are not multiples of the channel group.
+    S = 20 and 36 have S/2 not a multiple of 4: the column-form degridder's
+    lanes then change column at different steps (divergent P updates)."""
     from idg_gb300 import datasets as D
     from idg_gb300 import ops, tuning
 
