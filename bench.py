@@ -235,7 +235,7 @@ def run_ours(args, rank, world, local_rank):
     import torch
 
     from idg_gb300 import datasets as D
-    from idg_gb300 import ops
+    from idg_gb300 import hostmem, ops
 
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
@@ -285,6 +285,65 @@ def run_ours(args, rank, world, local_rank):
         rows_s = int(obs.metadata["time_offset"][ns - 1] + obs.metadata["nr_timesteps"][ns - 1])
         tune = tuning.autotune(nogrid, md[:ns], uvw[:rows_s], k, vis[:rows_s], None, at, sub[:ns], vis_out[:rows_s],
                                repeats=2, stream=stream, store=False)
+
+    # e2e through idg_imaging_cycle on page-locked host buffers (huge-page
+    # backed, idg_gb300.hostmem), with the tuned shapes, before the
+    # device-resident legs.  Every rank locks its visibilities in and out;
+    # when the ranks of this node would not fit in the host memory available,
+    # the e2e leg uses the leading subgrids that do (and says so), instead of
+    # failing.
+    e2e = None
+    cpu = None
+    vis_host = None
+    locked = []
+    local_world = int(os.environ.get("LOCAL_WORLD_SIZE", world))
+    e2e_n, e2e_rows = e2e_prefix(obs.metadata, spec.n_rows, 2 * C * 32,
+                                 0.6 * host_mem_available() / max(1, local_world))
+    if not args.no_e2e or rank == 0:
+        huge0 = hostmem.huge_page_bytes()
+        vis_host = hostmem.pinned_empty((e2e_rows,) + tuple(vis.shape[1:]), np.complex64)
+        locked.append(vis_host)
+        torch.from_numpy(vis_host).copy_(vis[:e2e_rows])
+    if not args.no_e2e:
+        out_host = hostmem.pinned_empty(vis_host.shape, np.complex64)
+        chunk = max(1, e2e_n // 32)
+        aterms_np = hostmem.pinned_copy(obs.aterms)
+        md_e2e = hostmem.pinned_copy(obs.metadata[:e2e_n])
+        uvw_e2e = hostmem.pinned_copy(obs.uvw[:e2e_rows])
+        locked += [out_host, aterms_np, md_e2e, uvw_e2e]
+        huge = hostmem.huge_page_bytes() - huge0
+        nvis_e2e = int(md_e2e["nr_timesteps"].astype(np.int64).sum()) * C
+        ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, vis_host, obs.taper, aterms_np, out_host,
+                          variant=variant, chunk_subgrids=chunk)  # warm (allocates device buffers)
+        totals = []
+        if dist:
+            dist.barrier()
+        for _ in range(args.steps):
+            t = ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, vis_host, obs.taper, aterms_np,
+                                  out_host, variant=variant, chunk_subgrids=chunk)
+            totals.append(t)
+        e2e_ms = float(np.mean([t["total_ms"] for t in totals]))
+        if dist:
+            tt = torch.tensor([e2e_ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_ms = float(tt.item())
+        e2e = {"value": world * nvis_e2e / (e2e_ms * 1e-3) / 1e6, "unit": "Mvis/s",
+               "h2d_bytes_per_step": int(totals[-1]["h2d_bytes"]), "d2h_bytes_per_step": int(totals[-1]["d2h_bytes"]),
+               "ms_per_step": e2e_ms,
+               "api": "idg_imaging_cycle (C ABI), page-locked huge-page host buffers (idg_gb300.hostmem)",
+               "host_buffers_gb": round(sum(x.nbytes for x in locked) / 1e9, 2),
+               "host_huge_pages_gb": round(huge / 1e9, 2),
+               "subgrids": e2e_n,
+               "chunks": (e2e_n + chunk - 1) // chunk,
+               "gridding_ms": float(np.mean([t["gridding_ms"] for t in totals])),
+               "degridding_ms": float(np.mean([t["degridding_ms"] for t in totals])),
+               "steps_ms": [round(float(t["total_ms"]), 1) for t in totals]}
+        # free the cycle's device buffers and the e2e inputs
+        ops.release_buffers()
+        for a in locked[1:]:
+            hostmem.release(a)
+        locked = locked[:1]
+        del out_host, aterms_np, md_e2e, uvw_e2e
 
     def step(v=variant, ev=None):
         # gridding step
@@ -430,54 +489,6 @@ def run_ours(args, rank, world, local_rank):
         plain = {"value": nvis / (pms * 1e-3) / 1e6, "unit": "Mvis/s", "ms_per_step": pms,
                  "gridder_ms": pe[0].elapsed_time(pe[1]), "degridder_ms": pe[5].elapsed_time(pe[6])}
 
-    # e2e through idg_imaging_cycle on pinned host buffers.  Every rank pins its
-    # visibilities in and out; when the ranks of this node would not fit in the
-    # host memory available, the e2e leg uses the leading subgrids that do (and
-    # says so), instead of failing.
-    e2e = None
-    cpu = None
-    vis_host = None
-    local_world = int(os.environ.get("LOCAL_WORLD_SIZE", world))
-    e2e_n, e2e_rows = e2e_prefix(obs.metadata, spec.n_rows, 2 * C * 32,
-                                 0.6 * host_mem_available() / max(1, local_world))
-    if not args.no_e2e or rank == 0:
-        vis_host = torch.empty((e2e_rows,) + tuple(vis.shape[1:]), dtype=vis.dtype, pin_memory=True)
-        vis_host.copy_(vis[:e2e_rows])
-    del sub, grid, vis_out
-    torch.cuda.empty_cache()
-    if not args.no_e2e:
-        out_host = torch.empty(vis_host.shape, dtype=vis.dtype, pin_memory=True)
-        chunk = max(1, e2e_n // 32)
-        aterms_np = np.ascontiguousarray(obs.aterms)
-        md_e2e = np.ascontiguousarray(obs.metadata[:e2e_n])
-        uvw_e2e = np.ascontiguousarray(obs.uvw[:e2e_rows])
-        nvis_e2e = int(md_e2e["nr_timesteps"].astype(np.int64).sum()) * C
-        ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, vis_host, obs.taper, aterms_np, out_host,
-                          variant=variant, chunk_subgrids=chunk)  # warm (allocates device buffers)
-        totals = []
-        if dist:
-            dist.barrier()
-        for _ in range(args.steps):
-            t = ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, vis_host, obs.taper, aterms_np,
-                                  out_host, variant=variant, chunk_subgrids=chunk)
-            totals.append(t)
-        e2e_ms = float(np.mean([t["total_ms"] for t in totals]))
-        if dist:
-            tt = torch.tensor([e2e_ms], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_ms = float(tt.item())
-        e2e = {"value": world * nvis_e2e / (e2e_ms * 1e-3) / 1e6, "unit": "Mvis/s",
-               "h2d_bytes_per_step": int(totals[-1]["h2d_bytes"]), "d2h_bytes_per_step": int(totals[-1]["d2h_bytes"]),
-               "ms_per_step": e2e_ms, "api": "idg_imaging_cycle (C ABI), pinned host buffers",
-               "subgrids": e2e_n,
-               "chunks": (e2e_n + chunk - 1) // chunk,
-               "gridding_ms": float(np.mean([t["gridding_ms"] for t in totals])),
-               "degridding_ms": float(np.mean([t["degridding_ms"] for t in totals])),
-               "steps_ms": [round(float(t["total_ms"]), 1) for t in totals]}
-        # cross-check: the host cycle reproduces the device-resident step's visibilities
-        ops.release_buffers()
-        del out_host
-
     # serving: a Poisson stream of gridding and degridding jobs of mixed sizes
     serving = None
     if not args.no_serve:
@@ -489,7 +500,10 @@ def run_ours(args, rank, world, local_rank):
         del jobs
 
     if rank == 0 and not args.skip_cpu:
-        cpu = cpu_baseline(obs, vis_host.numpy() if vis_host is not None else None, args.cpu_seconds)
+        cpu = cpu_baseline(obs, vis_host, args.cpu_seconds)
+    for a in locked:
+        hostmem.release(a)
+    del locked, vis_host
 
     if dist:
         dist.barrier()

@@ -422,6 +422,56 @@ def test_plan_steps_and_graph_cycle_match_direct_calls(oracle_mod, idg):
         plan.close()
 
 
+@pytest.mark.parametrize("chunk", [0, 5])
+@pytest.mark.parametrize("locked", [False, True])
+def test_host_buffer_cycle_matches_device_steps(idg, chunk, locked):
+    """idg_imaging_cycle on host buffers (pageable numpy arrays, or page-locked
+    huge-page arrays from idg_gb300.hostmem), in one chunk or in chunks of 5
+    subgrids with the copies overlapping the kernels, gives the grid and the
+    visibilities of the device-resident gridding and degridding steps."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import hostmem, ops
+
+    spec = D.config1()
+    spec.aterm_sigma = 0.05
+    obs = D.make_observation(spec)
+    vis = _vis(spec, seed=37)
+    S, G, N = spec.subgrid_size, spec.grid_size, spec.n_subgrids
+    gs = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    d = {k: dev(v) for k, v in dict(md=obs.metadata, uvw=obs.uvw, k=obs.wavenumbers, vis=vis, taper=obs.taper,
+                                    at=obs.aterms).items()}
+    sub = torch.empty((N, 4, S, S), dtype=torch.complex64, device="cuda")
+    g_ref = torch.zeros((1, 4, G, G), dtype=torch.complex64, device="cuda")
+    ops.grid_visibilities(gs, d["md"], d["uvw"], d["k"], d["vis"], d["taper"], d["at"], sub, g_ref)
+    v_ref = torch.zeros_like(d["vis"])
+    ops.degrid_visibilities(gs, d["md"], d["uvw"], d["k"], v_ref, d["taper"], d["at"], sub, g_ref)
+    torch.cuda.synchronize()
+
+    if locked:
+        host = [hostmem.pinned_copy(a) for a in (obs.metadata, obs.uvw, vis, obs.aterms)]
+        md_h, uvw_h, vis_h, at_h = host
+        out_h = hostmem.pinned_empty(vis.shape, np.complex64)
+        grid_h = hostmem.pinned_empty((1, 4, G, G), np.complex64)
+        host += [out_h, grid_h]
+    else:
+        host = []
+        md_h, uvw_h, vis_h, at_h = obs.metadata, obs.uvw, vis, obs.aterms
+        out_h = np.zeros(vis.shape, np.complex64)
+        grid_h = np.zeros((1, 4, G, G), np.complex64)
+    try:
+        for _ in range(2):  # the second call reuses the cycle's device buffers
+            t = ops.imaging_cycle(gs, md_h, uvw_h, obs.wavenumbers, vis_h, obs.taper, at_h, out_h, grid_out=grid_h,
+                                  chunk_subgrids=chunk)
+        check_rel(f"host cycle grid chunk={chunk} locked={locked}", grid_h, g_ref.cpu().numpy(), TOL)
+        check_rel(f"host cycle vis chunk={chunk} locked={locked}", out_h, v_ref.cpu().numpy(), TOL)
+        assert t["h2d_bytes"] >= vis.nbytes and t["d2h_bytes"] >= vis.nbytes + grid_h.nbytes
+        assert t["total_ms"] > 0 and t["gridding_ms"] > 0 and t["degridding_ms"] > 0
+    finally:
+        ops.release_buffers()
+        for a in host:
+            hostmem.release(a)
+
+
 def test_degenerate_plan_entries_every_batched_shape(oracle_mod, idg):
     """Every batched launch shape on plan entries at the edges of what a plan may
     hold: zero and one timestep, empty and one-channel ranges, ranges starting

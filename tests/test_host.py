@@ -231,3 +231,26 @@ def test_e2e_leg_fits_the_host_memory(idg):
     n, rows = bench.e2e_prefix(obs.metadata, spec.n_rows, row, (3 * T + T // 2) * row)
     assert (n, rows) == (3, 3 * T)
     assert bench.e2e_prefix(obs.metadata, spec.n_rows, row, 1.0)[0] == 1
+
+
+def test_hostmem_arrays_without_registration():
+    """idg_gb300.hostmem on a host without a GPU: the huge-page-advised mapping
+    gives zeroed C-contiguous arrays of any dtype and shape; release() of an
+    array that was never registered is a no-op."""
+    from idg_gb300 import hostmem
+    import idg_gb300._lib as L
+
+    a = hostmem.pinned_empty((3, 5, 4), np.complex64, register=False)
+    assert a.shape == (3, 5, 4) and a.dtype == np.complex64 and a.flags["C_CONTIGUOUS"] and a.flags["WRITEABLE"]
+    assert not a.any()
+    a[...] = 1 + 2j
+    assert (a == 1 + 2j).all()
+    md = np.zeros(7, L.METADATA_DTYPE)
+    md["nr_timesteps"] = np.arange(7)
+    b = hostmem.pinned_copy(md, register=False)
+    assert b.dtype == L.METADATA_DTYPE and (b["nr_timesteps"] == np.arange(7)).all()
+    assert np.ascontiguousarray(b, dtype=L.METADATA_DTYPE) is b  # passed to the C ABI without a copy
+    e = hostmem.pinned_empty(0, np.float32, register=False)
+    assert e.shape == (0,)
+    for x in (a, b, e, a[1:]):
+        hostmem.release(x)
