@@ -254,3 +254,30 @@ def test_hostmem_arrays_without_registration():
     assert e.shape == (0,)
     for x in (a, b, e, a[1:]):
         hostmem.release(x)
+
+
+def test_reference_arm_line(idg, monkeypatch):
+    """bench.py --impl reference: rank 0 returns one line with the contract's
+    keys (impl, value, zero copy bytes in its e2e block, a cpu_baseline that
+    describes the run); the other ranks return nothing.  The CPU sample is cut
+    to 0.2 s per half here."""
+    import argparse
+    import importlib.util
+    import json
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec_b = importlib.util.spec_from_file_location("bench_under_test3", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec_b)
+    spec_b.loader.exec_module(bench)
+    real = bench.cpu_baseline
+    monkeypatch.setattr(bench, "cpu_baseline", lambda obs, vis, target_s: real(obs, vis, 0.2))
+    args = argparse.Namespace(workload="config1", steps=2, warmup=1)
+    out = bench.run_reference(args, 0, 1)
+    json.dumps(out)
+    assert out["impl"] == "reference" and out["unit"] == "Mvis/s" and out["value"] > 0
+    assert out["higher_is_better"] is True and out["steps"] == 2 and out["warmup"] == 1
+    assert out["e2e"] == {"value": out["value"], "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    cb = out["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == out["value"] and cb["sample"]
+    assert out["config"]["workload"].startswith("config1")
+    assert bench.run_reference(args, 1, 2) is None
