@@ -8,6 +8,16 @@ import pytest
 from conftest import ROOT
 
 
+def _load_bench(name: str):
+    """bench.py imported as a module (it is a script at the repo root)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def test_yaml_subset_parses_reference_examples(idg, tmp_path):
     from idg_gb300 import config as C
 
@@ -193,13 +203,7 @@ def test_cpu_baseline_sample_stays_within_the_given_rows(idg):
     subgrid; however fast the host, the sample only uses subgrids whose rows
     are all in the visibilities it was given (a faster host once read past
     them)."""
-    import importlib.util
-    import os
-
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    spec_b = importlib.util.spec_from_file_location("bench_under_test", os.path.join(root, "bench.py"))
-    bench = importlib.util.module_from_spec(spec_b)
-    spec_b.loader.exec_module(bench)
+    bench = _load_bench("bench_under_test")
     from idg_gb300 import datasets as D
 
     spec = D.config1()
@@ -214,13 +218,7 @@ def test_e2e_leg_fits_the_host_memory(idg):
     """bench.py's e2e leg pins the visibilities in and out per rank; with too
     little host memory for all ranks of a node it takes the leading subgrids
     whose rows fit (whole plan otherwise)."""
-    import importlib.util
-    import os
-
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    spec_b = importlib.util.spec_from_file_location("bench_under_test2", os.path.join(root, "bench.py"))
-    bench = importlib.util.module_from_spec(spec_b)
-    spec_b.loader.exec_module(bench)
+    bench = _load_bench("bench_under_test2")
     from idg_gb300 import datasets as D
 
     spec = D.config1()
@@ -262,13 +260,9 @@ def test_reference_arm_line(idg, monkeypatch):
     describes the run); the other ranks return nothing.  The CPU sample is cut
     to 0.2 s per half here."""
     import argparse
-    import importlib.util
     import json
 
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    spec_b = importlib.util.spec_from_file_location("bench_under_test3", os.path.join(root, "bench.py"))
-    bench = importlib.util.module_from_spec(spec_b)
-    spec_b.loader.exec_module(bench)
+    bench = _load_bench("bench_under_test3")
     real = bench.cpu_baseline
     monkeypatch.setattr(bench, "cpu_baseline", lambda obs, vis, target_s: real(obs, vis, 0.2))
     args = argparse.Namespace(workload="config1", steps=2, warmup=1)
