@@ -13,10 +13,12 @@ touches it and registers it with cudaHostRegister; `release` unregisters it.
 from __future__ import annotations
 
 import mmap
+import threading
 
 import numpy as np
 
 _registered: dict[int, int] = {}  # data pointer -> registered bytes
+_lock = threading.Lock()
 
 
 def _cudart():
@@ -47,7 +49,8 @@ def pinned_empty(shape, dtype, register: bool = True) -> np.ndarray:
         rc = _cudart().cudaHostRegister(ptr, size, 0)
         if int(getattr(rc, "value", rc)) != 0:
             raise RuntimeError(f"cudaHostRegister of {size} bytes failed: {rc}")
-        _registered[ptr] = size
+        with _lock:
+            _registered[ptr] = size
     return arr
 
 
@@ -66,7 +69,9 @@ def release(arr: np.ndarray) -> None:
     while isinstance(base.base, np.ndarray):
         base = base.base
     ptr = base.ctypes.data
-    if _registered.pop(ptr, None) is not None:
+    with _lock:
+        size = _registered.pop(ptr, None)
+    if size is not None:
         _cudart().cudaHostUnregister(ptr)
 
 
