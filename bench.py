@@ -70,8 +70,12 @@ def parse():
     ap.add_argument("--max-subgrids", type=int, default=0, help="use only the first N subgrids of the plan (profiling)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (p50/p99 latency) leg")
     ap.add_argument("--serve-jobs", type=int, default=30, help="observations in the serving leg (2 jobs each)")
-    ap.add_argument("--serve-rate", type=float, default=16.0, help="mean arrival rate of the serving leg, jobs/s")
+    ap.add_argument("--serve-rates", default="4,16,32", help="mean arrival rates of the serving leg, jobs/s")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the batched-uneven (50,000 mixed subgrids) leg")
     ap.add_argument("--shapes", default="", help="G,D: batched gridder/degridder launch shapes instead of autotuning")
+    ap.add_argument("--host-buffers", choices=["auto", "pinned", "hostmem"], default="auto",
+                    help="page-locked host buffers of the e2e leg: cudaHostAlloc (pinned), huge-page memory "
+                         "registered with cudaHostRegister (hostmem), or whichever copies faster (auto)")
     return ap.parse_args()
 
 
@@ -229,6 +233,90 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+# host buffers of the e2e leg
+# ---------------------------------------------------------------------------
+def copy_probe(host_in, host_out, dev_buf, stream, chunks=32) -> dict:
+    """Plain cudaMemcpyAsync rates (GB/s) between two page-locked host arrays
+    and a device buffer of the same size: the whole array in `chunks` copies,
+    host to device, then device to host, each timed with CUDA events."""
+    import torch
+
+    hi = torch.from_numpy(host_in).view(torch.uint8).reshape(-1)
+    ho = torch.from_numpy(host_out).view(torch.uint8).reshape(-1)
+    d = dev_buf.view(torch.uint8).reshape(-1)
+    n = min(hi.numel(), d.numel())
+    step = max(1, n // chunks)
+    rates = {}
+    for direction in ("h2d", "d2h"):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for c0 in range(0, n, step):
+                sl = slice(c0, min(n, c0 + step))
+                if direction == "h2d":
+                    d[sl].copy_(hi[sl], non_blocking=True)
+                else:
+                    ho[sl].copy_(d[sl], non_blocking=True)
+            e1.record(stream)
+        e1.synchronize()
+        rates[direction + "_gbs"] = round(n / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+    return rates
+
+
+def e2e_host_buffers(kind: str, shape, fill, dev_buf, stream):
+    """The e2e leg's input and output visibility arrays, page-locked.
+
+    "pinned": cudaHostAlloc (torch pin_memory); "hostmem": transparent-huge-
+    page memory registered with cudaHostRegister (idg_gb300.hostmem); "auto":
+    pinned, unless its copy probe runs below 100 GB/s either way and hostmem
+    then probes faster.  The two kinds copy at the same rate on a healthy host
+    (about 210 GB/s in, 190 GB/s out on GB300), but either has been seen to
+    fall well below that in some processes.  Returns (vis_in, vis_out, record);
+    the record names the kind and holds every probe taken."""
+    import torch
+
+    from idg_gb300 import hostmem
+
+    def make(k):
+        if k == "pinned":
+            a = torch.empty(shape, dtype=torch.complex64, pin_memory=True).numpy()
+            b = torch.empty(shape, dtype=torch.complex64, pin_memory=True).numpy()
+        else:
+            a = hostmem.pinned_empty(shape, np.complex64)
+            b = hostmem.pinned_empty(shape, np.complex64)
+        torch.from_numpy(a).copy_(fill)
+        copy_probe(a, b, dev_buf, stream)  # first touch of the pages by the copy engines
+        return a, b, copy_probe(a, b, dev_buf, stream)
+
+    def drop(k, a, b):
+        if k == "hostmem":
+            hostmem.release(a)
+            hostmem.release(b)
+
+    first = "hostmem" if kind == "hostmem" else "pinned"
+    a, b, pr = make(first)
+    record = {"kind": first, "probes": {first: pr}}
+    room = host_mem_available() > 1.5 * (a.nbytes + b.nbytes)
+    if kind == "auto" and min(pr["h2d_gbs"], pr["d2h_gbs"]) < 100.0 and room:
+        a2, b2, pr2 = make("hostmem")
+        record["probes"]["hostmem"] = pr2
+        if min(pr2.values()) > min(pr.values()):
+            drop(first, a, b)
+            a, b, record["kind"] = a2, b2, "hostmem"
+        else:
+            drop("hostmem", a2, b2)
+    return a, b, record
+
+
+def release_host_buffers(record, *arrays):
+    from idg_gb300 import hostmem
+
+    if record["kind"] == "hostmem":
+        for a in arrays:
+            hostmem.release(a)
+
+
+# ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
 def run_ours(args, rank, world, local_rank):
@@ -286,35 +374,33 @@ def run_ours(args, rank, world, local_rank):
         tune = tuning.autotune(nogrid, md[:ns], uvw[:rows_s], k, vis[:rows_s], None, at, sub[:ns], vis_out[:rows_s],
                                repeats=2, stream=stream, store=False)
 
-    # e2e through idg_imaging_cycle on page-locked host buffers (huge-page
-    # backed, idg_gb300.hostmem), with the tuned shapes, before the
-    # device-resident legs.  Every rank locks its visibilities in and out;
-    # when the ranks of this node would not fit in the host memory available,
-    # the e2e leg uses the leading subgrids that do (and says so), instead of
-    # failing.
+    # e2e through idg_imaging_cycle on page-locked host buffers, with the tuned
+    # shapes, before the device-resident legs.  Every rank locks its
+    # visibilities in and out; when the ranks of this node would not fit in
+    # the host memory available, the e2e leg uses the leading subgrids that do
+    # (and says so), instead of failing.  The host buffers' copy rate is probed
+    # (plain cudaMemcpyAsync, the visibilities in 32 chunks each way) just
+    # before the leg, and each cycle reports the rate its own copies ran at.
     e2e = None
     cpu = None
     vis_host = None
-    locked = []
+    small = []  # page-locked plan, uvw and A-terms of the e2e leg
+    host_rec = None
     local_world = int(os.environ.get("LOCAL_WORLD_SIZE", world))
     e2e_n, e2e_rows = e2e_prefix(obs.metadata, spec.n_rows, 2 * C * 32,
                                  0.6 * host_mem_available() / max(1, local_world))
-    if not args.no_e2e or rank == 0:
-        huge0 = hostmem.huge_page_bytes()
-        vis_host = hostmem.pinned_empty((e2e_rows,) + tuple(vis.shape[1:]), np.complex64)
-        locked.append(vis_host)
-        torch.from_numpy(vis_host).copy_(vis[:e2e_rows])
     if not args.no_e2e:
-        out_host = hostmem.pinned_empty(vis_host.shape, np.complex64)
+        vis_host, out_host, host_rec = e2e_host_buffers(args.host_buffers, (e2e_rows,) + tuple(vis.shape[1:]),
+                                                        vis[:e2e_rows], vis_out[:e2e_rows], stream)
         chunk = max(1, e2e_n // 32)
         aterms_np = hostmem.pinned_copy(obs.aterms)
         md_e2e = hostmem.pinned_copy(obs.metadata[:e2e_n])
         uvw_e2e = hostmem.pinned_copy(obs.uvw[:e2e_rows])
-        locked += [out_host, aterms_np, md_e2e, uvw_e2e]
-        huge = hostmem.huge_page_bytes() - huge0
+        small = [aterms_np, md_e2e, uvw_e2e]
         nvis_e2e = int(md_e2e["nr_timesteps"].astype(np.int64).sum()) * C
-        ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, vis_host, obs.taper, aterms_np, out_host,
-                          variant=variant, chunk_subgrids=chunk)  # warm (allocates device buffers)
+        for _ in range(2):  # warm: allocates the cycle's device buffers
+            ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, vis_host, obs.taper, aterms_np, out_host,
+                              variant=variant, chunk_subgrids=chunk)
         totals = []
         if dist:
             dist.barrier()
@@ -327,23 +413,30 @@ def run_ours(args, rank, world, local_rank):
             tt = torch.tensor([e2e_ms], device=dev)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             e2e_ms = float(tt.item())
+        steps_ms = [float(t["total_ms"]) for t in totals]
         e2e = {"value": world * nvis_e2e / (e2e_ms * 1e-3) / 1e6, "unit": "Mvis/s",
                "h2d_bytes_per_step": int(totals[-1]["h2d_bytes"]), "d2h_bytes_per_step": int(totals[-1]["d2h_bytes"]),
                "ms_per_step": e2e_ms,
-               "api": "idg_imaging_cycle (C ABI), page-locked huge-page host buffers (idg_gb300.hostmem)",
-               "host_buffers_gb": round(sum(x.nbytes for x in locked) / 1e9, 2),
-               "host_huge_pages_gb": round(huge / 1e9, 2),
+               "api": "idg_imaging_cycle (C ABI) on page-locked host buffers",
+               "host_buffers": host_rec["kind"],
+               "copy_probe_gbs": host_rec["probes"],
+               "h2d_gbs_steps": [round(t["h2d_vis_bytes"] / (t["h2d_vis_ms"] * 1e-3) / 1e9, 1) for t in totals],
+               "d2h_gbs_steps": [round(t["d2h_vis_bytes"] / (t["d2h_vis_ms"] * 1e-3) / 1e9, 1) for t in totals],
+               "host_buffers_gb": round((vis_host.nbytes + out_host.nbytes + sum(x.nbytes for x in small)) / 1e9, 2),
                "subgrids": e2e_n,
                "chunks": (e2e_n + chunk - 1) // chunk,
                "gridding_ms": float(np.mean([t["gridding_ms"] for t in totals])),
                "degridding_ms": float(np.mean([t["degridding_ms"] for t in totals])),
-               "steps_ms": [round(float(t["total_ms"]), 1) for t in totals]}
-        # free the cycle's device buffers and the e2e inputs
+               "steps_ms": [round(x, 1) for x in steps_ms],
+               "steps_spread": round((max(steps_ms) - min(steps_ms)) / e2e_ms, 4)}
+        # free the cycle's device buffers and the e2e inputs (vis_host stays for the CPU baseline)
         ops.release_buffers()
-        for a in locked[1:]:
+        for a in small:
             hostmem.release(a)
-        locked = locked[:1]
-        del out_host, aterms_np, md_e2e, uvw_e2e
+        release_host_buffers(host_rec, out_host)
+        del out_host, aterms_np, md_e2e, uvw_e2e, small
+    elif rank == 0 and not args.skip_cpu:
+        vis_host = vis[:e2e_rows].cpu().numpy()
 
     def step(v=variant, ev=None):
         # gridding step
@@ -489,21 +582,33 @@ def run_ours(args, rank, world, local_rank):
         plain = {"value": nvis / (pms * 1e-3) / 1e6, "unit": "Mvis/s", "ms_per_step": pms,
                  "gridder_ms": pe[0].elapsed_time(pe[1]), "degridder_ms": pe[5].elapsed_time(pe[6])}
 
-    # serving: a Poisson stream of gridding and degridding jobs of mixed sizes
+    # serving: Poisson streams of gridding and degridding jobs of mixed sizes,
+    # one per arrival rate, over the same observations
     serving = None
     if not args.no_serve:
         from idg_gb300 import serve_bench
 
         srng = np.random.default_rng(5 + rank)
         jobs = [serve_bench.make_observation(srng, 2e7) for _ in range(args.serve_jobs)]
-        serving = serve_bench.run_stream(jobs, args.serve_rate, slots=4, budget_gb=64.0, seed=5 + rank)
+        serving = [serve_bench.run_stream(jobs, float(r), slots=4, budget_gb=64.0, seed=5 + rank)
+                   for r in args.serve_rates.split(",")]
         del jobs
+
+    # batched uneven: 50,000 subgrids of mixed size, time span and channel
+    # group, one CUDA graph per cycle, against the plain kernels
+    uneven = None
+    if not args.no_uneven and world == 1:
+        from idg_gb300 import uneven_bench
+
+        del sub, vis_out  # room for the job's own buffers
+        torch.cuda.empty_cache()
+        uneven = uneven_bench.run(uneven_bench.parse(["--steps", "3", "--warmup", "3"]))
 
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(obs, vis_host, args.cpu_seconds)
-    for a in locked:
-        hostmem.release(a)
-    del locked, vis_host
+    if host_rec is not None:
+        release_host_buffers(host_rec, vis_host)
+    del vis_host
 
     if dist:
         dist.barrier()
@@ -531,6 +636,7 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "plain": plain,
         "serving": serving,
+        "uneven": uneven,
         "imaging": imaging,
         "clocks": clock_info,
     }

@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define IDG_ABI_VERSION 1
+#define IDG_ABI_VERSION 2
 
 typedef enum idg_status {
     IDG_OK = 0,
@@ -140,12 +140,22 @@ IDG_API int idg_gridder(const idg_params *params, int variant, int64_t nr_subgri
  * and result as idg_gridder().  Limits: at most 2^30 subgrids; calls on one
  * device share the array, so calls whose kernels could overlap on the GPU
  * must be serialised by the caller; a rejected plan entry yields a zero
- * subgrid (its check bit is not reported).  The first call on a device looks
- * up the array's address and should come before any stream capture there. */
+ * subgrid and sets a bit that idg_noalloc_status() reports.  The first call on
+ * a device does a one-time set-up: it looks up the array's address and loads
+ * the kernels (under CUDA's lazy loading a kernel is otherwise loaded at its
+ * first launch, and loading takes device memory).  Make that first call --
+ * with nr_subgrids = 0 it does the set-up alone -- before the caller's pool
+ * takes the device memory and before any stream capture on that device. */
 IDG_API int idg_gridder_noalloc(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
                                 const idg_subgrid_ext *ext, int64_t nr_rows, const float *uvw,
                                 const float *wavenumbers, const void *visibilities, const float *spheroidal,
                                 const void *aterms, void *subgrids, void *stream);
+/* The check word of the last idg_gridder_noalloc() call on the current device
+ * (bit 0: a plan entry named rows, stations, A-terms or channels out of range
+ * and its subgrid was left zero), read after synchronising `stream`.  Each
+ * call clears the word when it starts.  Allocates nothing.  No counterpart in
+ * the reference. */
+IDG_API int idg_noalloc_status(void *stream, uint32_t *status);
 
 /* Degridder: V[t,c] = sum_pixels A(taper * subgrid) e^{-i phi}; writes only
  * the rows/channels the plan names.  Replaces kernel_degridder_v6
@@ -345,6 +355,12 @@ typedef struct idg_job_stats {
     int64_t visibilities;
     int32_t status;
     int32_t reserved;
+    /* Device interval of the job's kernels (first kernel queued .. last kernel
+     * done), in ms since the server was created, from CUDA events on the job's
+     * slot stream; -1 when not recorded.  Intervals of two jobs that intersect
+     * show that their kernels ran on the GPU at the same time. */
+    double device_start_ms;
+    double device_end_ms;
 } idg_job_stats;
 
 typedef struct idg_server_stats {
@@ -358,8 +374,14 @@ IDG_API int idg_server_create(const idg_server_config *config, idg_server **serv
 /* Finishes the queued and running jobs, then frees everything. */
 IDG_API int idg_server_destroy(idg_server *server);
 IDG_API int idg_server_grid_create(idg_server *server, int32_t grid_size, int32_t nr_w_planes, int64_t *grid_id);
-/* Copies a grid to the host after the jobs running on it. */
+/* Copies a grid to the host after every job on it that was submitted before
+ * this call (it waits for them to be admitted, then for them to finish, on a
+ * stream of its own; it returns when the copy is done).  Gridding jobs on that
+ * grid are not admitted while the copy runs; degridding jobs may run beside
+ * it. */
 IDG_API int idg_server_grid_read(idg_server *server, int64_t grid_id, void *host_out);
+/* Frees a grid; IDG_ERR_REJECTED while jobs are queued or running on it or a
+ * read of it is in progress. */
 IDG_API int idg_server_grid_release(idg_server *server, int64_t grid_id);
 IDG_API int idg_server_submit(idg_server *server, const idg_job *job, int64_t *job_id);
 /* Waits at most timeout_ms for a job (IDG_ERR_TIMEOUT otherwise); returns the job's status. */
@@ -374,6 +396,14 @@ typedef struct idg_cycle_timing {
     int64_t h2d_bytes;
     int64_t d2h_bytes;
     int64_t kernel_launches;
+    /* The visibility copies alone: h2d_vis_ms is the time the copies in took
+     * on their stream, where they run back to back; d2h_vis_ms is the sum of
+     * the durations of the copies out (each starts when its chunk is
+     * degridded).  bytes / ms gives the host copy rate the cycle saw. */
+    double h2d_vis_ms;
+    double d2h_vis_ms;
+    int64_t h2d_vis_bytes;
+    int64_t d2h_vis_bytes;
 } idg_cycle_timing;
 
 /* One imaging cycle on HOST buffers: copies the plan, uvw, wavenumbers,
@@ -384,7 +414,10 @@ typedef struct idg_cycle_timing {
  * overlap the kernels (the plan's rows must then be in chunk order; otherwise
  * the cycle runs as one chunk).  Device buffers are kept between calls of
  * the same sizes and freed by idg_release_buffers().  Pinned host buffers
- * give full copy bandwidth. */
+ * give full copy bandwidth.  The cycle clears the device check word (see
+ * idg_device_status) before its first kernel and returns IDG_ERR_DEVICE_CHECK
+ * when one of its own kernels set it.  Every return, an error included, comes
+ * after all of the call's copies from and into the host buffers have ended. */
 IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_subgrids,
                               const idg_metadata *metadata, int64_t nr_rows, const float *uvw,
                               const float *wavenumbers, const void *visibilities_in, const float *spheroidal,

@@ -884,9 +884,16 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
 //  20: mirror quads, 64 threads x 4 quads, 4 CTAs/SM (8 warps), unrolled by two (whole passes for S = 32)
 //  21: mirror quads, 128 threads x 4 quads, 2 CTAs/SM (8 warps), unrolled by two (whole passes for S = 64)
 //  22: shape 20 with the channel loop unrolled by four
+// load_only: only make sure the kernel is loaded into the current context
+// (under lazy module loading a kernel is otherwise loaded, which takes device
+// memory, at its first launch).
 template <int NT, int PAIRS, int TV, int MINB, int PIPE>
-cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
+cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream, bool load_only) {
     auto kern = gridder_fast_kernel<NT, PAIRS, TV, MINB, PIPE>;
+    if (load_only) {
+        cudaFuncAttributes fa;
+        return cudaFuncGetAttributes(&fa, kern);
+    }
     const size_t smem = layout(a.S, a.C, TV).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -905,9 +912,13 @@ cudaError_t launch_shape(const KernelArgs &a, cudaStream_t stream) {
 }
 
 template <int NT, int GP, int TV, int MINB, int UNR>
-cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
-    if (a.S % 2 != 0) return cudaErrorInvalidValue;
+cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream, bool load_only) {
     auto kern = gridder_quad_kernel<NT, GP, TV, MINB, UNR>;
+    if (load_only) {
+        cudaFuncAttributes fa;
+        return cudaFuncGetAttributes(&fa, kern);
+    }
+    if (a.S % 2 != 0) return cudaErrorInvalidValue;
     const size_t smem = layout(a.S, a.C, TV).total + (size_t)NT * GP * 3 * sizeof(f2); // + quad geometry
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -929,32 +940,45 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
 
 int gridder_fast_shapes() { return 23; }
 
-cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
+namespace {
+cudaError_t dispatch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape, bool load_only) {
     switch (shape) {
-    case 1: return launch_shape<128, 4, 256, 2, 1>(a, stream);
-    case 2: return launch_shape<128, 2, 128, 4, 1>(a, stream);
-    case 3: return launch_shape<256, 2, 256, 2, 1>(a, stream);
-    case 4: return launch_shape<128, 2, 128, 4, 0>(a, stream);
-    case 5: return launch_shape<128, 4, 256, 3, 2>(a, stream);
-    case 6: return launch_shape<128, 4, 256, 2, 3>(a, stream);
-    case 7: return launch_shape<128, 4, 256, 2, kGauss | kUnroll2>(a, stream);
-    case 8: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll2>(a, stream);
-    case 9: return launch_shape<256, 2, 256, 2, kGauss | kUnroll2>(a, stream);
-    case 10: return launch_shape<128, 4, 256, 3, kGauss>(a, stream);
-    case 11: return launch_shape<96, 3, 256, 3, kGauss | kPipe | kUnroll2>(a, stream);
-    case 12: return launch_shape<128, 3, 256, 2, kGauss | kPipe | kUnroll2>(a, stream);
-    case 13: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll4>(a, stream);
-    case 14: return launch_shape<128, 4, 256, 2, kGauss | kUnroll4>(a, stream);
-    case 15: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kUnroll4>(a, stream);
-    case 16: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kPipe | kUnroll4>(a, stream);
-    case 17: return launch_shape<128, 3, 256, 2, kGauss | kRecur | kUnroll4>(a, stream);
-    case 18: return launch_quad<128, 1, 256, 3, 4>(a, stream);
-    case 19: return launch_quad<128, 1, 256, 2, 4>(a, stream);
-    case 20: return launch_quad<64, 2, 256, 4, 2>(a, stream);
-    case 21: return launch_quad<128, 2, 256, 2, 2>(a, stream);
-    case 22: return launch_quad<64, 2, 256, 4, 4>(a, stream);
-    default: return launch_shape<128, 4, 256, 3, 0>(a, stream);
+    case 1: return launch_shape<128, 4, 256, 2, 1>(a, stream, load_only);
+    case 2: return launch_shape<128, 2, 128, 4, 1>(a, stream, load_only);
+    case 3: return launch_shape<256, 2, 256, 2, 1>(a, stream, load_only);
+    case 4: return launch_shape<128, 2, 128, 4, 0>(a, stream, load_only);
+    case 5: return launch_shape<128, 4, 256, 3, 2>(a, stream, load_only);
+    case 6: return launch_shape<128, 4, 256, 2, 3>(a, stream, load_only);
+    case 7: return launch_shape<128, 4, 256, 2, kGauss | kUnroll2>(a, stream, load_only);
+    case 8: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll2>(a, stream, load_only);
+    case 9: return launch_shape<256, 2, 256, 2, kGauss | kUnroll2>(a, stream, load_only);
+    case 10: return launch_shape<128, 4, 256, 3, kGauss>(a, stream, load_only);
+    case 11: return launch_shape<96, 3, 256, 3, kGauss | kPipe | kUnroll2>(a, stream, load_only);
+    case 12: return launch_shape<128, 3, 256, 2, kGauss | kPipe | kUnroll2>(a, stream, load_only);
+    case 13: return launch_shape<128, 4, 256, 2, kGauss | kPipe | kUnroll4>(a, stream, load_only);
+    case 14: return launch_shape<128, 4, 256, 2, kGauss | kUnroll4>(a, stream, load_only);
+    case 15: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kUnroll4>(a, stream, load_only);
+    case 16: return launch_shape<128, 4, 256, 2, kGauss | kRecur | kPipe | kUnroll4>(a, stream, load_only);
+    case 17: return launch_shape<128, 3, 256, 2, kGauss | kRecur | kUnroll4>(a, stream, load_only);
+    case 18: return launch_quad<128, 1, 256, 3, 4>(a, stream, load_only);
+    case 19: return launch_quad<128, 1, 256, 2, 4>(a, stream, load_only);
+    case 20: return launch_quad<64, 2, 256, 4, 2>(a, stream, load_only);
+    case 21: return launch_quad<128, 2, 256, 2, 2>(a, stream, load_only);
+    case 22: return launch_quad<64, 2, 256, 4, 4>(a, stream, load_only);
+    default: return launch_shape<128, 4, 256, 3, 0>(a, stream, load_only);
     }
+}
+} // namespace
+
+cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape) {
+    return dispatch_gridder_fast(a, stream, shape, false);
+}
+
+cudaError_t load_gridder_fast() {
+    const KernelArgs a{};
+    for (int shape = 0; shape < gridder_fast_shapes(); ++shape)
+        if (cudaError_t e = dispatch_gridder_fast(a, nullptr, shape, true)) return e;
+    return cudaSuccess;
 }
 
 } // namespace idg

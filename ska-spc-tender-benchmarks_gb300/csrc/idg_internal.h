@@ -15,6 +15,9 @@ cudaError_t launch_degridder(const KernelArgs &a, int variant, int max_nc, cudaS
 // shape: index into the batched gridder's launch shapes (see gridder_fast_shapes()).
 cudaError_t launch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape);
 int gridder_fast_shapes();
+// Loads the kernels of every batched gridder shape into the current device's
+// context without launching them.
+cudaError_t load_gridder_fast();
 // The shape the batched gridder uses on the current device for subgrid size S.
 int batched_gridder_shape(int S);
 void set_batched_gridder_shape(int S, int shape);

@@ -17,10 +17,17 @@
 // stream before the launch.  All calls on a device share the array, so calls
 // whose kernels overlap on the GPU (other streams, no ordering between them)
 // race on the work counter and must be serialised by the caller.  A plan
-// entry the kernel rejects yields an all-zero subgrid; its check bit stays in
-// the array (idg_device_status() reports the other entry points' word only).
-// The first call on a device also looks up the array's device address; make
-// that first call before any stream capture on that device.
+// entry the kernel rejects yields an all-zero subgrid and sets bit 0 of the
+// check word, which idg_noalloc_status() reads (idg_device_status() reports
+// the other entry points' word only).
+// The first call on a device does a one-time set-up there: it looks up the
+// array's device address and loads the batched gridder's kernels into the
+// context.  Under CUDA's lazy module loading both would otherwise happen at
+// first use, and loading a module takes device memory -- which fails in the
+// very case this entry point is for, a pool that already owns all of it.
+// So make the first call on a device before the caller's pool takes the
+// device memory, and before any stream capture on that device; a call with
+// nr_subgrids = 0 does the set-up alone.
 #include <mutex>
 #include <vector>
 
@@ -41,7 +48,8 @@ std::mutex g_addr_mutex;
 std::vector<void *> g_addr; // per device: address of g_noalloc_scratch
 
 // Set-up, once per device, with that device current: fetch the array's device
-// address (host code cannot use the symbol itself as a pointer).
+// address (host code cannot use the symbol itself as a pointer) and load the
+// kernels this entry point launches.
 int scratch_address(void **out) {
     int dev = 0;
     IDG_CUDA(cudaGetDevice(&dev));
@@ -51,6 +59,8 @@ int scratch_address(void **out) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return idg::cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        e = idg::load_gridder_fast();
+        if (e != cudaSuccess) return idg::cuda_fail(e, "loading the batched gridder's kernels");
         g_addr[dev] = p;
     }
     *out = g_addr[dev];
@@ -74,6 +84,8 @@ extern "C" IDG_API int idg_gridder_noalloc(const idg_params *params, int64_t nr_
                     "nr_subgrids %lld exceeds %lld, the most the allocation-free gridder's 32-bit work counter "
                     "can schedule",
                     (long long)nr_subgrids, (long long)kMaxSubgrids);
+    void *scratch = nullptr;
+    if (int rc = scratch_address(&scratch)) return rc;
     if (nr_subgrids == 0) return IDG_OK;
     if (nr_rows < 0) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_rows %lld < 0", (long long)nr_rows);
     if (!metadata || !uvw || !wavenumbers || !visibilities || !aterms || !subgrids)
@@ -83,8 +95,6 @@ extern "C" IDG_API int idg_gridder_noalloc(const idg_params *params, int64_t nr_
     if (!aligned16(visibilities) || !aligned16(aterms) || !aligned16(subgrids))
         return fail(IDG_ERR_INVALID_ARGUMENT, "visibilities, aterms and subgrids must be 16-byte aligned");
 
-    void *scratch = nullptr;
-    if (int rc = scratch_address(&scratch)) return rc;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     IDG_CUDA(cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned int), st));
 
@@ -112,5 +122,17 @@ extern "C" IDG_API int idg_gridder_noalloc(const idg_params *params, int64_t nr_
     a.status = reinterpret_cast<unsigned *>(scratch) + 1;
     cudaError_t e = launch_gridder_fast(a, st, batched_gridder_shape(a.S));
     if (e != cudaSuccess) return cuda_fail(e, "allocation-free gridder launch");
+    return IDG_OK;
+}
+
+extern "C" IDG_API int idg_noalloc_status(void *stream, uint32_t *status) {
+    using namespace idg;
+    if (!status) return fail(IDG_ERR_INVALID_ARGUMENT, "status is NULL");
+    void *scratch = nullptr;
+    if (int rc = scratch_address(&scratch)) return rc;
+    IDG_CUDA(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)));
+    unsigned word = 0;
+    IDG_CUDA(cudaMemcpy(&word, reinterpret_cast<unsigned *>(scratch) + 1, sizeof word, cudaMemcpyDeviceToHost));
+    *status = word;
     return IDG_OK;
 }

@@ -191,14 +191,36 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     if (int rc = new_event(&t_deg1, true)) return rc;
     if (int rc = new_event(&t_end, true)) return rc;
     if (int rc = new_event(&consts_in, false)) return rc;
-    std::vector<cudaEvent_t> h2d_done(nchunks), deg_done(nchunks);
+    // copy timing: the visibility copies in run back to back on s_h2d
+    // (h2d_v0 .. h2d_v1); each copy out is bracketed on s_d2h (d2h_b, d2h_e)
+    cudaEvent_t h2d_v0, h2d_v1;
+    if (int rc = new_event(&h2d_v0, true)) return rc;
+    if (int rc = new_event(&h2d_v1, true)) return rc;
+    std::vector<cudaEvent_t> h2d_done(nchunks), deg_done(nchunks), d2h_b(nchunks), d2h_e(nchunks);
     for (size_t i = 0; i < nchunks; ++i) {
         if (int rc = new_event(&h2d_done[i], false)) return rc;
         if (int rc = new_event(&deg_done[i], false)) return rc;
+        if (int rc = new_event(&d2h_b[i], true)) return rc;
+        if (int rc = new_event(&d2h_e[i], true)) return rc;
     }
 
+    DeviceWords w;
+    if (int rc = device_words(&w)) return rc;
     IDG_CUDA(cudaDeviceSynchronize());
-    int64_t launches = 0, h2d = 0, d2h = 0;
+    // From here on every return -- early ones included -- first waits for the
+    // cycle's streams, so that no copy from or into the caller's host buffers
+    // is still queued when the call returns.  (Declared after the event guard,
+    // so it runs before the events are destroyed.)
+    struct StreamGuard {
+        cudaStream_t s[3];
+        ~StreamGuard() {
+            for (cudaStream_t x : s) cudaStreamSynchronize(x);
+        }
+    } stream_guard{{B.s_h2d, B.s_compute, B.s_d2h}};
+    // The check word is library-wide: clear what earlier, unrelated calls left
+    // in it, so that the status read at the end is this cycle's own.
+    IDG_CUDA(cudaMemsetAsync(w.status, 0, sizeof(unsigned), B.s_compute));
+    int64_t launches = 0, h2d = 0, d2h = 0, h2d_vis = 0, d2h_vis = 0;
     IDG_CUDA(cudaEventRecord(t_start, B.s_h2d));
     // constants first (small), then visibility chunks
     IDG_CUDA(cudaMemcpyAsync(B.md, metadata, b_md, cudaMemcpyHostToDevice, B.s_h2d));
@@ -208,13 +230,16 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     IDG_CUDA(cudaMemcpyAsync(B.aterms, aterms, b_aterms, cudaMemcpyHostToDevice, B.s_h2d));
     h2d += b_md + b_uvw + b_k + b_taper + b_aterms;
     IDG_CUDA(cudaEventRecord(consts_in, B.s_h2d));
+    IDG_CUDA(cudaEventRecord(h2d_v0, B.s_h2d));
     for (size_t i = 0; i < nchunks; ++i) {
         const size_t off = (size_t)c_rows0[i] * C * 32, bytes = (size_t)(c_rows1[i] - c_rows0[i]) * C * 32;
         IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.vis_in) + off, static_cast<const char *>(visibilities_in) + off,
                                  bytes, cudaMemcpyHostToDevice, B.s_h2d));
         h2d += bytes;
+        h2d_vis += bytes;
         IDG_CUDA(cudaEventRecord(h2d_done[i], B.s_h2d));
     }
+    IDG_CUDA(cudaEventRecord(h2d_v1, B.s_h2d));
 
     // gridding phase
     IDG_CUDA(cudaStreamWaitEvent(B.s_compute, consts_in, 0));
@@ -246,9 +271,12 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         IDG_CUDA(cudaEventRecord(deg_done[i], B.s_compute));
         IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, deg_done[i], 0));
         const size_t off = (size_t)c_rows0[i] * C * 32, bytes = (size_t)(c_rows1[i] - c_rows0[i]) * C * 32;
+        IDG_CUDA(cudaEventRecord(d2h_b[i], B.s_d2h));
         IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(visibilities_out) + off, static_cast<char *>(B.vis_out) + off,
                                  bytes, cudaMemcpyDeviceToHost, B.s_d2h));
+        IDG_CUDA(cudaEventRecord(d2h_e[i], B.s_d2h));
         d2h += bytes;
+        d2h_vis += bytes;
     }
     IDG_CUDA(cudaEventRecord(t_deg1, B.s_compute));
     if (grid_out) {
@@ -260,8 +288,6 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     IDG_CUDA(cudaEventSynchronize(t_end));
     IDG_CUDA(cudaStreamSynchronize(B.s_compute));
 
-    DeviceWords w;
-    if (int rc = device_words(&w)) return rc;
     unsigned status = 0;
     IDG_CUDA(cudaMemcpy(&status, w.status, sizeof status, cudaMemcpyDeviceToHost));
     if (status) {
@@ -279,6 +305,18 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         timing->h2d_bytes = h2d;
         timing->d2h_bytes = d2h;
         timing->kernel_launches = launches;
+        float hv = 0;
+        IDG_CUDA(cudaEventElapsedTime(&hv, h2d_v0, h2d_v1));
+        double dv = 0;
+        for (size_t i = 0; i < nchunks; ++i) {
+            float x = 0;
+            IDG_CUDA(cudaEventElapsedTime(&x, d2h_b[i], d2h_e[i]));
+            dv += x;
+        }
+        timing->h2d_vis_ms = hv;
+        timing->d2h_vis_ms = dv;
+        timing->h2d_vis_bytes = h2d_vis;
+        timing->d2h_vis_bytes = d2h_vis;
     }
     return IDG_OK;
 }

@@ -47,6 +47,7 @@ struct Grid {
     int32_t size = 0, planes = 1;
     int last_op = -1;                  // op of the jobs currently holding the grid
     std::vector<cudaEvent_t> holders;  // their completion events
+    int readers = 0;                   // idg_server_grid_read calls copying the grid out
 };
 
 struct Job {
@@ -61,6 +62,8 @@ struct Job {
     int slot = -1;
     void *arena = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t k0 = nullptr, k1 = nullptr; // around the job's kernels (timing events)
+    double dev_start_ms = -1, dev_end_ms = -1; // k0, k1 relative to the server's epoch event
     int status = IDG_OK;
     bool finished = false;
 };
@@ -101,6 +104,7 @@ struct idg_server {
     std::map<int64_t, std::shared_ptr<Job>> jobs;
     std::vector<std::shared_ptr<Job>> slots;
     std::vector<cudaStream_t> streams;
+    cudaEvent_t epoch = nullptr; // recorded at creation: origin of the jobs' device intervals
     std::map<int64_t, Grid> grids;
     int64_t next_job = 1, next_grid = 1;
     size_t in_use = 0, peak_use = 0;
@@ -216,6 +220,7 @@ void idg_server::launch(Job &j) {
     if (g.last_op != -1 && g.last_op != j.spec.op)
         for (cudaEvent_t h : g.holders) chk(cudaStreamWaitEvent(st, h, 0));
 
+    if (j.k0) chk(cudaEventRecord(j.k0, st));
     if (j.spec.op == IDG_JOB_GRID) {
         chk(launch_gridder(a, variant, p.nr_channels, st));
         chk(launch_subgrid_fft(a.subgrids, (int64_t)N, p.subgrid_size, +1, a.taper, st));
@@ -226,8 +231,10 @@ void idg_server::launch(Job &j) {
                             static_cast<const float2 *>(g.dev), a.subgrids, st));
         chk(launch_subgrid_fft(a.subgrids, (int64_t)N, p.subgrid_size, -1, a.taper, st));
         chk(launch_degridder(a, variant, p.nr_channels, st));
-        chk(cudaMemcpyAsync(j.spec.vis_out, dp(L.vis), b_vis, cudaMemcpyDeviceToHost, st));
     }
+    if (j.k1) chk(cudaEventRecord(j.k1, st));
+    if (j.spec.op == IDG_JOB_DEGRID)
+        chk(cudaMemcpyAsync(j.spec.vis_out, dp(L.vis), b_vis, cudaMemcpyDeviceToHost, st));
     chk(cudaEventRecord(j.done, st));
     if (g.last_op != j.spec.op) g.holders.clear();
     g.last_op = j.spec.op;
@@ -248,7 +255,9 @@ void idg_server::admit_locked() {
             }
         if (free_slot < 0) return;
         Job &j = **it;
-        if (is_blocked(j.spec.grid_id) || in_use + j.footprint > (size_t)cfg.hbm_budget_bytes) {
+        // a gridding job must not change a grid while idg_server_grid_read copies it out
+        const bool grid_being_read = j.spec.op == IDG_JOB_GRID && grids[j.spec.grid_id].readers > 0;
+        if (is_blocked(j.spec.grid_id) || grid_being_read || in_use + j.footprint > (size_t)cfg.hbm_budget_bytes) {
             blocked.push_back(j.spec.grid_id);
             ++it; // a smaller job behind it, on another grid, may fit now
             continue;
@@ -269,8 +278,14 @@ void idg_server::admit_locked() {
         in_use += j.footprint;
         peak_use = std::max(peak_use, in_use);
         cudaEventCreateWithFlags(&j.done, cudaEventDisableTiming);
+        if (cudaEventCreate(&j.k0) != cudaSuccess || cudaEventCreate(&j.k1) != cudaSuccess) {
+            cudaGetLastError();
+            if (j.k0) cudaEventDestroy(j.k0);
+            j.k0 = j.k1 = nullptr; // the job runs without its device interval
+        }
         launch(j);
         it = queue.erase(it);
+        cv_done.notify_all(); // a grid read may be waiting for this job's admission
     }
 }
 
@@ -278,11 +293,28 @@ void idg_server::poll_locked() {
     for (int s = 0; s < (int)slots.size(); ++s) {
         auto &jp = slots[s];
         if (!jp) continue;
-        cudaError_t q = jp->status == IDG_OK ? cudaEventQuery(jp->done) : cudaSuccess;
+        // The slot's stream holds only this job's work (and earlier, finished
+        // work): the job is over when the stream is idle.  Querying the stream
+        // rather than the job's event also covers a launch that failed part way,
+        // whose later copies and kernels may still be queued.
+        cudaError_t q = cudaStreamQuery(streams[s]);
         if (q == cudaErrorNotReady) continue;
         Job &j = *jp;
         j.t_done = Clock::now();
         if (q != cudaSuccess && j.status == IDG_OK) j.status = cuda_fail(q, "server job");
+        if (j.k0 && j.k1 && q == cudaSuccess && j.status == IDG_OK) {
+            float t0 = 0, t1 = 0;
+            if (cudaEventElapsedTime(&t0, epoch, j.k0) == cudaSuccess &&
+                cudaEventElapsedTime(&t1, epoch, j.k1) == cudaSuccess) {
+                j.dev_start_ms = t0;
+                j.dev_end_ms = t1;
+            } else {
+                cudaGetLastError();
+            }
+        }
+        if (j.k0) cudaEventDestroy(j.k0);
+        if (j.k1) cudaEventDestroy(j.k1);
+        j.k0 = j.k1 = nullptr;
         // plan entries the kernels rejected
         if (j.status == IDG_OK) {
             unsigned st = 0;
@@ -348,6 +380,14 @@ IDG_API int idg_server_create(const idg_server_config *cfg, idg_server **out) {
             return cuda_fail(e, "server stream");
         }
     }
+    if (cudaEventCreate(&srv->epoch) != cudaSuccess || cudaEventRecord(srv->epoch, srv->streams[0]) != cudaSuccess ||
+        cudaEventSynchronize(srv->epoch) != cudaSuccess) {
+        cudaError_t e = cudaGetLastError();
+        if (srv->epoch) cudaEventDestroy(srv->epoch);
+        for (auto &t : srv->streams) cudaStreamDestroy(t);
+        delete srv;
+        return cuda_fail(e, "server epoch event");
+    }
     // keep freed job memory in the pool between jobs
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, srv->device) == cudaSuccess) {
@@ -370,6 +410,7 @@ IDG_API int idg_server_destroy(idg_server *srv) {
     cudaSetDevice(srv->device);
     for (auto &g : srv->grids) cudaFree(g.second.dev);
     for (auto &s : srv->streams) cudaStreamDestroy(s);
+    cudaEventDestroy(srv->epoch);
     delete srv;
     return IDG_OK;
 }
@@ -392,16 +433,57 @@ IDG_API int idg_server_grid_create(idg_server *srv, int32_t grid_size, int32_t n
 
 IDG_API int idg_server_grid_read(idg_server *srv, int64_t grid_id, void *host_out) {
     if (!srv || !host_out) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL argument");
-    std::unique_lock<std::mutex> lock(srv->mu);
-    auto it = srv->grids.find(grid_id);
-    if (it == srv->grids.end()) return fail(IDG_ERR_NOT_FOUND, "unknown grid %lld", (long long)grid_id);
-    std::vector<cudaEvent_t> wait = it->second.holders;
-    void *dev = it->second.dev;
-    const size_t bytes = it->second.bytes;
-    lock.unlock();
-    cudaSetDevice(srv->device);
-    for (cudaEvent_t e : wait) cudaEventSynchronize(e);
-    IDG_CUDA(cudaMemcpy(host_out, dev, bytes, cudaMemcpyDeviceToHost));
+    IDG_CUDA(cudaSetDevice(srv->device));
+    // The read covers every job on the grid submitted before it: first wait
+    // until those have all been admitted.  The copy then runs on a stream of
+    // its own.  Under the lock that stream is made to wait for every job now
+    // holding the grid (the scheduler destroys a holder's event only under the
+    // same lock), and the grid is marked as being read: until the copy ends,
+    // the scheduler admits no gridding job on it and idg_server_grid_release
+    // refuses it.
+    cudaStream_t rs = nullptr;
+    IDG_CUDA(cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking));
+    void *dev = nullptr;
+    size_t bytes = 0;
+    {
+        std::unique_lock<std::mutex> lock(srv->mu);
+        const int64_t last_job = srv->next_job - 1;
+        auto queued_before = [&] {
+            for (auto &q : srv->queue)
+                if (q->spec.grid_id == grid_id && q->id <= last_job) return true;
+            return false;
+        };
+        if (!srv->cv_done.wait_for(lock, std::chrono::minutes(10), [&] { return !queued_before(); })) {
+            cudaStreamDestroy(rs);
+            return fail(IDG_ERR_TIMEOUT, "grid %lld: earlier jobs not admitted within 10 minutes", (long long)grid_id);
+        }
+        auto it = srv->grids.find(grid_id);
+        if (it == srv->grids.end()) {
+            cudaStreamDestroy(rs);
+            return fail(IDG_ERR_NOT_FOUND, "unknown grid %lld", (long long)grid_id);
+        }
+        Grid &g = it->second;
+        cudaError_t e = cudaSuccess;
+        for (cudaEvent_t h : g.holders)
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(rs, h, 0);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(rs);
+            return cuda_fail(e, "grid read: wait for the grid's jobs");
+        }
+        ++g.readers;
+        dev = g.dev;
+        bytes = g.bytes;
+    }
+    cudaError_t e = cudaMemcpyAsync(host_out, dev, bytes, cudaMemcpyDeviceToHost, rs);
+    const cudaError_t e2 = cudaStreamSynchronize(rs);
+    if (e == cudaSuccess) e = e2;
+    cudaStreamDestroy(rs);
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        --srv->grids[grid_id].readers;
+    }
+    srv->cv_work.notify_all(); // gridding jobs held back by the read may start
+    if (e != cudaSuccess) return cuda_fail(e, "grid read");
     return IDG_OK;
 }
 
@@ -411,6 +493,7 @@ IDG_API int idg_server_grid_release(idg_server *srv, int64_t grid_id) {
     auto it = srv->grids.find(grid_id);
     if (it == srv->grids.end()) return fail(IDG_ERR_NOT_FOUND, "unknown grid %lld", (long long)grid_id);
     if (!it->second.holders.empty()) return fail(IDG_ERR_REJECTED, "grid %lld has jobs in flight", (long long)grid_id);
+    if (it->second.readers > 0) return fail(IDG_ERR_REJECTED, "grid %lld is being read", (long long)grid_id);
     for (auto &q : srv->queue)
         if (q->spec.grid_id == grid_id) return fail(IDG_ERR_REJECTED, "grid %lld has queued jobs", (long long)grid_id);
     cudaSetDevice(srv->device);
@@ -474,6 +557,8 @@ IDG_API int idg_server_wait(idg_server *srv, int64_t job_id, int64_t timeout_ms,
         stats->latency_ms = ms_between(j->t_submit, j->t_done);
         stats->visibilities = j->nvis;
         stats->status = j->status;
+        stats->device_start_ms = j->dev_start_ms;
+        stats->device_end_ms = j->dev_end_ms;
     }
     srv->jobs.erase(job_id);
     if (j->status != IDG_OK) return fail(j->status, "job %lld failed", (long long)job_id);

@@ -97,6 +97,10 @@ class IdgCycleTiming(ctypes.Structure):
         ("h2d_bytes", ctypes.c_int64),
         ("d2h_bytes", ctypes.c_int64),
         ("kernel_launches", ctypes.c_int64),
+        ("h2d_vis_ms", ctypes.c_double),
+        ("d2h_vis_ms", ctypes.c_double),
+        ("h2d_vis_bytes", ctypes.c_int64),
+        ("d2h_vis_bytes", ctypes.c_int64),
     ]
 
 
@@ -131,6 +135,8 @@ class IdgJobStats(ctypes.Structure):
         ("visibilities", ctypes.c_int64),
         ("status", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+        ("device_start_ms", ctypes.c_double),
+        ("device_end_ms", ctypes.c_double),
     ]
 
 
@@ -187,6 +193,7 @@ _SIGNATURES = {
     "idg_device_status": [_P, ctypes.POINTER(ctypes.c_uint32), _I32],
     "idg_gridder": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
     "idg_gridder_noalloc": [ctypes.POINTER(IdgParams), _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
+    "idg_noalloc_status": [_P, ctypes.POINTER(ctypes.c_uint32)],
     "idg_degridder": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P],
     "idg_subgrid_fft": [ctypes.POINTER(IdgParams), _I64, _I32, _P, _P, _P],
     "idg_adder": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],

@@ -206,8 +206,7 @@ def imaging_cycle(spec: GridSpec, metadata: np.ndarray, uvw: np.ndarray, wavenum
     _lib.call("idg_imaging_cycle", ctypes.byref(p), variant, md.shape[0], ptr(md), uvw.shape[0], ptr(uvw),
               ptr(wavenumbers), ptr(vis_in), ptr(taper), ptr(aterms), ptr(vis_out), ptr(grid_out),
               int(chunk_subgrids), ctypes.byref(t))
-    return {"total_ms": t.total_ms, "gridding_ms": t.gridding_ms, "degridding_ms": t.degridding_ms,
-            "h2d_bytes": t.h2d_bytes, "d2h_bytes": t.d2h_bytes, "kernel_launches": t.kernel_launches}
+    return {f: getattr(t, f) for f, _ in _lib.IdgCycleTiming._fields_}
 
 
 def plan_subgrids(uvw, frequencies, baselines, nr_timesteps: int, subgrid_size: int, grid_size: int,

@@ -116,7 +116,8 @@ class Server:
                 self._inflight.pop(int(job_id), None)
         _lib.check(rc)
         return {"queue_ms": st.queue_ms, "run_ms": st.run_ms, "latency_ms": st.latency_ms,
-                "visibilities": st.visibilities}
+                "visibilities": st.visibilities, "device_start_ms": st.device_start_ms,
+                "device_end_ms": st.device_end_ms}
 
     def stats(self) -> dict:
         s = IdgServerSummary()

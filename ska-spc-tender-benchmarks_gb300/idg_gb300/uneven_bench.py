@@ -30,14 +30,18 @@ from . import datasets as D
 from . import ops, tuning
 
 
-def main(argv=None):
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--subgrids", type=int, default=50000)
     ap.add_argument("--stations", type=int, default=2000)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--seed", type=int, default=4)
-    args = ap.parse_args(argv)
+    return ap.parse_args(argv)
+
+
+def run(args) -> dict:
+    """Builds the job, times both forms and returns the result line."""
     dev = torch.device("cuda")
     parts = D.config4(n_subgrids=args.subgrids, nstations=args.stations, seed=args.seed)
     G = parts[0].spec.grid_size
@@ -119,10 +123,15 @@ def main(argv=None):
         "steps": args.steps,
         "warmup": args.warmup,
     }
-    print(json.dumps(line), flush=True)
     cyc.close()
     for _, _, p in groups:
         p.close()
+    return line
+
+
+def main(argv=None):
+    line = run(parse(argv))
+    print(json.dumps(line), flush=True)
     return line
 
 

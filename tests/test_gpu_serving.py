@@ -1,7 +1,9 @@
-"""Serving: jobs admitted while others run give the same results as the same
+"""Serving: jobs admitted while others run -- their kernels overlapping on the
+GPU, shown by the jobs' device intervals -- give the same results as the same
 jobs run alone (within the parity tolerance -- the adder accumulates with
-floating-point atomics, so the grid's summation order may differ), jobs
-larger than the HBM budget are rejected, and latency statistics are kept."""
+floating-point atomics, so the grid's summation order may differ), a grid can
+be read while jobs on it are still running, jobs larger than the HBM budget
+are rejected, and latency statistics are kept."""
 import numpy as np
 import pytest
 import torch
@@ -33,27 +35,36 @@ def _job(seed, nstations, ntimesteps, nchannels, grid_size=1024):
     return grid_in, degrid
 
 
-JOBS = [(1, 6, 128, 16), (2, 9, 96, 8), (3, 5, 256, 24), (4, 8, 64, 16)]
+# (seed, stations, timesteps, channels): 600-1150 subgrids of 32 timesteps each,
+# large enough that a job's kernels run for a good part of a millisecond
+JOBS = [(1, 16, 256, 16), (2, 20, 192, 8), (3, 12, 512, 24), (4, 18, 128, 16)]
 
 
 def _run(server, jobs, together):
-    """Grid every job into its own resident grid, then degrid from it."""
-    from idg_gb300.serving import Server  # noqa: F401
-
+    """Grid every job into its own resident grid, then degrid from it.
+    Returns the grids and visibilities, and each job's statistics."""
     grids = [server.grid_create(1024) for _ in jobs]
+    stats = []
     if together:
         ids = [server.submit(L.IDG_JOB_GRID, g, gid) for (g, _), gid in zip(jobs, grids)]
         ids += [server.submit(L.IDG_JOB_DEGRID, d, gid) for (_, d), gid in zip(jobs, grids)]
-        for i in ids:
-            server.wait(i, 120)
+        stats = [server.wait(i, 120) for i in ids]
     else:
         for (g, d), gid in zip(jobs, grids):
-            server.wait(server.submit(L.IDG_JOB_GRID, g, gid), 120)
-            server.wait(server.submit(L.IDG_JOB_DEGRID, d, gid), 120)
+            stats.append(server.wait(server.submit(L.IDG_JOB_GRID, g, gid), 120))
+            stats.append(server.wait(server.submit(L.IDG_JOB_DEGRID, d, gid), 120))
     out = [(server.grid_read(gid, 1024), d.vis.copy()) for (_, d), gid in zip(jobs, grids)]
     for gid in grids:
         server.grid_release(gid)
-    return out
+    return out, stats
+
+
+def _overlapping_pairs(stats):
+    """Pairs of jobs whose kernels' device intervals intersect."""
+    iv = [(s["device_start_ms"], s["device_end_ms"]) for s in stats]
+    assert all(0 <= a < b for a, b in iv), iv
+    return [(i, j) for i in range(len(iv)) for j in range(i + 1, len(iv))
+            if max(iv[i][0], iv[j][0]) < min(iv[i][1], iv[j][1])]
 
 
 def test_jobs_alone_and_in_the_mix_agree(idg):
@@ -61,13 +72,18 @@ def test_jobs_alone_and_in_the_mix_agree(idg):
 
     jobs = [_job(*j) for j in JOBS]
     with Server(max_slots=1, hbm_budget_bytes=8 << 30) as s1:
-        alone = _run(s1, jobs, together=False)
+        alone, job_alone = _run(s1, jobs, together=False)
         st1 = s1.stats()
+    # one slot: every job runs alone on the GPU
+    assert _overlapping_pairs(job_alone) == []
     for _, d in jobs:
         d.vis[...] = 0
     with Server(max_slots=4, hbm_budget_bytes=8 << 30, cta_share=True) as s4:
-        mixed = _run(s4, jobs, together=True)
+        mixed, job_mixed = _run(s4, jobs, together=True)
         st4 = s4.stats()
+    pairs = _overlapping_pairs(job_mixed)
+    print(f"[serving] jobs whose kernels overlapped on the GPU: {pairs}")
+    assert pairs, "no two jobs' kernels ran at the same time"
     for k, ((ga, va), (gm, vm)) in enumerate(zip(alone, mixed)):
         assert np.abs(ga).max() > 0 and np.abs(va).max() > 0
         check_rel(f"serving job {k} grid alone vs mix", gm, ga, TOL)
@@ -99,6 +115,28 @@ def test_serving_result_matches_direct_plan(idg):
     check_rel("served grid vs plan", grid_srv, grid.cpu().numpy(), TOL)
     check_rel("served vis vs plan", d.vis, vout.cpu().numpy(), TOL)
     plan.close()
+
+
+def test_grid_read_while_jobs_run(idg):
+    """grid_read called right after submission, while the gridding job runs,
+    waits for it and returns its complete grid; a read beside a running
+    degridding job (which does not change the grid) returns the same bytes."""
+    from idg_gb300.serving import Server
+
+    g, d = _job(11, 24, 512, 16)
+    with Server(max_slots=2, hbm_budget_bytes=8 << 30) as s:
+        gid = s.grid_create(1024)
+        jg = s.submit(L.IDG_JOB_GRID, g, gid)
+        early = s.grid_read(gid, 1024)
+        s.wait(jg, 120)
+        after = s.grid_read(gid, 1024)
+        jd = s.submit(L.IDG_JOB_DEGRID, d, gid)
+        beside = s.grid_read(gid, 1024)
+        s.wait(jd, 120)
+        s.grid_release(gid)
+    assert np.abs(after).max() > 0
+    assert np.array_equal(early, after)
+    assert np.array_equal(beside, after)
 
 
 def test_job_over_budget_is_rejected(idg):

@@ -5,9 +5,11 @@ static device array of the library, so the call allocates nothing.
 
 Checked through the C ABI against idg_gridder(IDG_VARIANT_BATCHED) on the
 same inputs, within the parity tolerance of the other tests, on two calls in a
-row (the second call must start from a cleared work counter).  This file is
-collected last so that a failure here leaves every other test already run;
-it also passes when run alone in a fresh process.
+row (the second call must start from a cleared work counter), with the
+device's free memory unchanged across the second call.  A rejected plan entry
+is reported by idg_noalloc_status().  This file is collected last so that a
+failure here leaves every other test already run; it also passes when run
+alone in a fresh process.
 """
 import ctypes
 
@@ -60,13 +62,27 @@ def test_noalloc_gridder_matches_batched_gridder():
     want = ref.cpu().numpy()
     p = gs.to_c()
     stream = torch.cuda.current_stream().cuda_stream
-    for call in range(2):
-        out = torch.full((N, 4, S, S), float("nan"), dtype=torch.complex64, device="cuda")
+    # the one-time set-up alone (an empty plan): address lookup, kernel loading
+    rc = lib.idg_gridder_noalloc(ctypes.byref(p), 0, None, None, 0, None, None, None, None, None, None, stream)
+    assert rc == L.IDG_OK, L.last_error()
+    outs = [torch.full((N, 4, S, S), float("nan"), dtype=torch.complex64, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    for call, out in enumerate(outs):
+        free0 = torch.cuda.mem_get_info()[0]
         rc = lib.idg_gridder_noalloc(ctypes.byref(p), N, t["md"].data_ptr(), None, spec.n_rows, t["uvw"].data_ptr(),
                                      t["k"].data_ptr(), t["vis"].data_ptr(), t["taper"].data_ptr(),
                                      t["at"].data_ptr(), out.data_ptr(), stream)
         assert rc == L.IDG_OK, L.last_error()
         torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info()[0]
+        print(f"[noalloc] call {call}: device free memory {free0} -> {free1} bytes")
+        if call == 1:
+            # the first launch of a kernel may still reserve local memory for it;
+            # a second call must take nothing
+            assert free1 == free0, f"device free memory changed by {free0 - free1} bytes"
+        st = ctypes.c_uint32(1 << 31)
+        assert lib.idg_noalloc_status(stream, ctypes.byref(st)) == L.IDG_OK, L.last_error()
+        assert st.value == 0
         got = out.cpu().numpy()
         assert np.isfinite(got.view(np.float32)).all(), f"call {call}: subgrids left unwritten"
         e = _rel(got, want)
@@ -81,3 +97,28 @@ def test_noalloc_gridder_rejects_oversized_plan():
                                  None)
     assert rc == L.IDG_ERR_UNSUPPORTED
     assert "2^30" in L.last_error() or "1073741824" in L.last_error()
+
+
+def test_noalloc_status_reports_a_rejected_entry():
+    """A plan entry naming a station outside the A-term table yields a zero
+    subgrid and bit 0 of idg_noalloc_status(); the next good call clears it."""
+    lib = L.load()
+    spec, gs, t = _inputs()
+    N, S = spec.n_subgrids, spec.subgrid_size
+    md_np = t["md"].cpu().numpy().copy()
+    bad = md_np.view(L.METADATA_DTYPE).reshape(-1)
+    bad["station1"][1] = spec.nstations  # out of range
+    md_bad = torch.from_numpy(md_np).cuda()
+    p = gs.to_c()
+    stream = torch.cuda.current_stream().cuda_stream
+    out = torch.full((N, 4, S, S), float("nan"), dtype=torch.complex64, device="cuda")
+    for md, want in ((md_bad, 1), (t["md"], 0)):
+        rc = lib.idg_gridder_noalloc(ctypes.byref(p), N, md.data_ptr(), None, spec.n_rows, t["uvw"].data_ptr(),
+                                     t["k"].data_ptr(), t["vis"].data_ptr(), t["taper"].data_ptr(),
+                                     t["at"].data_ptr(), out.data_ptr(), stream)
+        assert rc == L.IDG_OK, L.last_error()
+        st = ctypes.c_uint32(0)
+        assert lib.idg_noalloc_status(stream, ctypes.byref(st)) == L.IDG_OK, L.last_error()
+        assert st.value & 1 == want
+        if want:
+            assert np.abs(out[1].cpu().numpy()).max() == 0
