@@ -522,6 +522,15 @@ def run_ours(args, rank, world, local_rank):
         traffic = DRAM_BYTES_PER_SUBGRID[name] * N if S == 32 else None
         per_kernel[name] = {"achieved": ach / 1e12, "frac": ach / peak, "ms": ms, "traffic": traffic}
     dom = "degridder" if degrid_ms > grid_ms else "gridder"
+    # the measured FFMA peak against 128 FP32 lanes x 2 flop per SM clock, at
+    # the SM clock sampled over the timed region (the microbenchmark itself
+    # runs for milliseconds, below the sampler's 200 ms period)
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = clock_info["sm_mhz"] if clock_info else None
+    theory = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 if sm_mhz else None
+    peak_check = {"sms": props.multi_processor_count, "fp32_lanes_per_sm": 128, "sm_mhz": sm_mhz,
+                  "lanes_x_2_x_clock_tflops": theory / 1e12 if theory else None,
+                  "measured_over_lanes_x_2_x_clock": peak / theory if theory else None}
     roof = {
         "bound": "fp32",
         "kernel": dom,
@@ -536,6 +545,7 @@ def run_ours(args, rank, world, local_rank):
                        "carries HBM and bf16 figures, no FP32 FMA figure); the SFU bound (16 sin/cos per SM clock, 2 per "
                        "pixel-visibility) is within 2% of the FMA bound on GB300",
         "algorithmic": "34 flop (17 FMA) + 1 sincos per pixel-visibility; %.3g pixel-visibilities per launch" % pixvis,
+        "peak_check": peak_check,
         "gridder": per_kernel["gridder"],
         "degridder": per_kernel["degridder"],
         "kernel_ms": {n: float(np.mean(parts[:, j])) for j, n in enumerate(

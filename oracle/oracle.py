@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import re
 import subprocess
 
 import numpy as np
@@ -22,7 +23,27 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libidg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libidgref.so")
-REFERENCE_DIR = "/root/reference"
+
+
+def _reference_dir() -> str:
+    """Where the reference sources are: $IDG_REFERENCE_DIR when set, else the
+    default that oracle/Makefile (the recipe that compiles them) gives
+    IDG_REFERENCE_DIR; empty when neither names one."""
+    env = os.environ.get("IDG_REFERENCE_DIR", "")
+    if env:
+        return env
+    try:
+        with open(os.path.join(HERE, "Makefile")) as f:
+            for line in f:
+                m = re.match(r"\s*IDG_REFERENCE_DIR\s*\?=\s*(\S+)", line)
+                if m:
+                    return m.group(1)
+    except OSError:
+        pass
+    return ""
+
+
+REFERENCE_DIR = _reference_dir()
 
 # 36-byte plan entry, gridding/inc/types.hpp:7-25
 METADATA_DTYPE = np.dtype(
@@ -72,7 +93,7 @@ def build(with_ref: bool | None = None) -> None:
         os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
         subprocess.run(["gcc", "-std=gnu11", *_FLAGS, "-o", ORACLE_SO, src[0], "-lm"], check=True)
     if with_ref is None:
-        with_ref = os.path.isdir(REFERENCE_DIR)
+        with_ref = bool(REFERENCE_DIR) and os.path.isdir(REFERENCE_DIR)
     if with_ref:
         g = os.path.join(REFERENCE_DIR, "gridding")
         ref_src = [os.path.join(g, "src", f) for f in ("gridding_benchmark.cpp", "degridding_benchmark.cpp",

@@ -304,6 +304,66 @@ def config3(subgrid_size: int = 32, nstations: int = 100, ntimesteps: int = 8192
                            aterm_interval=256, seed=seed)
 
 
+def config3_sample(subgrid_size: int = 32, baselines_per_decile: int = 2, ntimesteps: int = 512,
+                   seed: int = 3, pick_seed: int = 17):
+    """A sample of the full config-3 geometry -- 100 stations in a disk 100 km
+    across, 8192 x 1 s, 64 channels over 100-200 MHz -- small enough for the
+    FP64 oracle: ``baselines_per_decile`` baselines drawn (seeded) from every
+    decile of baseline length over all 4950 baselines, plus the longest
+    baseline, each over the same window of ``ntimesteps`` steps of the 8192 (a
+    seeded offset on the 256-step A-term slot grid).  The stations are those
+    of ``make_observation(config3(...))`` (same seed); uvw is computed for the
+    picked baselines only, and the plan is split in channel and time
+    (``plan_subgrids_split``), rows numbered picked-baseline by picked-baseline.
+
+    Returns (obs, decile, edges, lengths): ``decile`` and ``lengths`` (metres)
+    per picked baseline, ``edges`` the nine decile boundaries (metres) of all
+    4950 baseline lengths.  obs.spec is the full config-3 spec with
+    ``ntimesteps`` = the window; its A-term table has the window's slots for all
+    100 stations."""
+    import dataclasses
+    import types
+
+    full = config3(subgrid_size, seed=seed)
+    rng = np.random.default_rng(full.seed)
+    st = stations_in_disk(full.nstations, full.disk_radius_m, rng)
+    bl_all = baseline_pairs(full.nstations)
+    enu_all = st[bl_all[:, 1]] - st[bl_all[:, 0]]
+    length = np.linalg.norm(enu_all, axis=1)
+    edges = np.quantile(length, np.linspace(0, 1, 11)[1:-1])
+    dec_all = np.searchsorted(edges, length, side="right")
+    prng = np.random.default_rng(pick_seed + subgrid_size)
+    picks = [int(np.argmax(length))]
+    for d in range(10):
+        cand = np.setdiff1d(np.where(dec_all == d)[0], picks)
+        picks += [int(x) for x in prng.choice(cand, min(baselines_per_decile, cand.size), replace=False)]
+    picks = np.array(sorted(picks))
+    interval = full.aterm_interval
+    t0 = int(prng.integers(0, (full.ntimesteps - ntimesteps) // interval + 1)) * interval
+    H = (np.arange(full.ntimesteps) - (full.ntimesteps - 1) / 2.0) * full.integration_s * EARTH_ROTATION_RATE
+    uvw = earth_rotation_uvw(enu_all[picks], H[t0:t0 + ntimesteps], np.deg2rad(full.dec_deg), np.deg2rad(full.lat_deg))
+    uvw = uvw.reshape(-1, 3).astype(np.float32)
+    freqs = np.linspace(full.f_start, full.f_end, full.nchannels)
+    k = (2 * np.pi * freqs / SPEED_OF_LIGHT).astype(np.float32)
+    spec = dataclasses.replace(full, ntimesteps=ntimesteps)
+    S = subgrid_size
+    at = np.zeros((spec.n_aterm_slots, spec.nstations, S, S, 4), np.complex64)
+    at[..., 0] = 1
+    at[..., 3] = 1
+    noise = prng.standard_normal((*at.shape, 2), dtype=np.float32)
+    at += (spec.aterm_sigma * (noise[..., 0] + 1j * noise[..., 1])).astype(np.complex64)
+    taper = pswf_taper(S, spec.taper_c)
+    bl = bl_all[picks]
+    # the planner walks len(picks) baselines of `ntimesteps` rows each
+    view = types.SimpleNamespace(n_baselines=len(picks), ntimesteps=ntimesteps, subgrid_size=S,
+                                 grid_size=spec.grid_size, image_size=spec.image_size,
+                                 timesteps_per_subgrid=spec.timesteps_per_subgrid, w_step=spec.w_step,
+                                 nr_w_planes=spec.nr_w_planes, aterm_interval=spec.aterm_interval)
+    md, ext = plan_subgrids_split(view, uvw, freqs, bl)
+    obs = Observation(spec, st, bl, uvw, freqs, k, at, taper, md, ext)
+    return obs, dec_all[picks], edges, length[picks]
+
+
 def config4(n_subgrids: int = 50000, nstations: int = 2000, sizes=(24, 32, 48), groups=(8, 16, 32, 64),
             seed: int = 4) -> list[Observation]:
     """The batched-uneven generator: `n_subgrids` subgrids sampled from the

@@ -1,8 +1,9 @@
 """The GPU planner (idg_plan_subgrids) against the host planner
 (datasets.plan_subgrids_split): every plan entry and channel range identical,
 bit for bit, on the config-3 generator (100 km baselines, 64 channels over
-100-200 MHz, S = 32 and 64) and on config-2 geometry (10 km, 16 channels,
-A-term slots every 256 steps)."""
+100-200 MHz, S = 32 and 64) -- shrunk to 12 stations, and as the sample of the
+full 100-station geometry that reaches 97.6 km -- and on config-2 geometry
+(10 km, 16 channels, A-term slots every 256 steps)."""
 import dataclasses
 
 import numpy as np
@@ -39,6 +40,27 @@ def test_gpu_plan_matches_host_plan(idg, case):
     for f in want_md.dtype.names:
         assert np.array_equal(md[f], want_md[f]), f
     assert np.array_equal(ext, want_ext)
+
+
+@pytest.mark.parametrize("S", [32, 64])
+def test_gpu_plan_matches_host_plan_at_100_km(idg, S):
+    """The longest baselines of the full config-3 geometry: at 200 MHz their
+    tracks cross a subgrid in under a minute and a channel group holds one to
+    four channels (S = 32)."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    obs, _, _, lengths = D.config3_sample(S)
+    spec = obs.spec
+    assert lengths.max() >= 95e3
+    md, ext = ops.plan_subgrids(torch.from_numpy(obs.uvw).cuda(), torch.from_numpy(obs.frequencies).cuda(),
+                                torch.from_numpy(obs.baselines.astype(np.int32)).cuda(), spec.ntimesteps, S,
+                                spec.grid_size, spec.image_size, spec.timesteps_per_subgrid, spec.aterm_interval)
+    print(f"[planner] config3 sample to {lengths.max() / 1e3:.1f} km, S={S}: {md.shape[0]} subgrids")
+    assert md.shape == obs.metadata.shape
+    for f in obs.metadata.dtype.names:
+        assert np.array_equal(md[f], obs.metadata[f]), f
+    assert np.array_equal(ext, obs.ext)
 
 
 def test_gpu_plan_reports_the_needed_capacity(idg):

@@ -1,14 +1,19 @@
-"""Precision sweep on the config-3 generator: baselines to 100 km, 64 channels
-over 100-200 MHz, subgrids of 32^2 and 64^2, planned with channel and time
-splitting (datasets.plan_subgrids_split).
+"""Precision sweep on the config-3 generator: the full 100-station geometry
+(a disk 100 km across, baselines to 97.6 km), 64 channels over 100-200 MHz,
+subgrids of 32^2 and 64^2, planned with channel and time splitting
+(datasets.plan_subgrids_split).
 
-For a seeded sample of subgrids from every baseline-length decile, the
+The sample (datasets.config3_sample) takes two baselines from every decile of
+baseline length over all 4950 baselines, plus the longest, over a 512-step
+window of the 8192-step observation, so that the FP64 oracle finishes in
+seconds; uvw is computed for those baselines only.  For a seeded sample of
+subgrids from every decile -- always including the longest baseline's -- the
 gridder's subgrids and the degridder's visibilities of both variants are
 compared with the FP64 oracle of the same gridder/degridder.  Relative RMS and
 maximum error (max |got - want| over the RMS of want) are printed per decile as
 one JSON line each, and the relative RMS is held to the 1e-5 tolerance overall
-and in every decile.  The observation is the config-3 generator shrunk to 12
-stations and 512 timesteps so that the FP64 oracle finishes in seconds.
+and in every decile.  This is where the reference's FP32 phase
+(gridding/src/gridding_benchmark.cpp:77-81, :118-124) cancels worst.
 """
 import json
 
@@ -39,23 +44,23 @@ def _decile_errors(got, want, decile, nd=10):
 
 
 def _sample(oracle_mod, S):
-    """Config-3 observation, a seeded sample of PER_DECILE subgrids per baseline
-    decile, random visibilities / subgrids and the FP64 oracle's outputs."""
+    """Config-3 sample, a seeded sample of PER_DECILE subgrids per baseline
+    decile (plus the longest baseline's first subgrids), random visibilities /
+    subgrids and the FP64 oracle's outputs."""
     from idg_gb300 import datasets as D
 
-    spec = D.config3(S, nstations=12, ntimesteps=512)
-    obs = D.make_observation(spec, split=True)
+    obs, bl_dec, edges, bl_len = D.config3_sample(S)
+    spec = obs.spec
     md_all, ext_all = obs.metadata, obs.ext
     C = spec.nchannels
-    # baseline length of every subgrid, deciles over subgrids
-    enu = obs.stations[obs.baselines[:, 1]] - obs.stations[obs.baselines[:, 0]]
-    blen = np.linalg.norm(enu, axis=1)
     sub_bl = md_all["time_offset"] // spec.ntimesteps
-    edges = np.quantile(blen[sub_bl], np.linspace(0, 1, 11)[1:-1])
-    dec_all = np.searchsorted(edges, blen[sub_bl], side="right")
+    dec_all = bl_dec[sub_bl]
+    longest = np.where(sub_bl == int(np.argmax(bl_len)))[0]
+    assert bl_len.max() >= 95e3 and bl_dec[np.argmax(bl_len)] == 9
     rng = np.random.default_rng(7 + S)
-    pick = np.sort(np.concatenate([rng.choice(np.where(dec_all == d)[0], min(PER_DECILE, int((dec_all == d).sum())),
-                                              replace=False) for d in range(10)]))
+    pick = np.concatenate([rng.choice(np.where(dec_all == d)[0], min(PER_DECILE, int((dec_all == d).sum())),
+                                      replace=False) for d in range(10)] + [longest[:4], longest[-4:]])
+    pick = np.unique(pick)
     md, ext, dec = md_all[pick].copy(), ext_all[pick].copy(), dec_all[pick]
     N = md.shape[0]
     rows = obs.uvw.shape[0]
@@ -69,12 +74,12 @@ def _sample(oracle_mod, S):
         r = slice(int(m["time_offset"]), int(m["time_offset"]) + int(m["nr_timesteps"]))
         covered[r, e["channel_begin"]:e["channel_end"]] = True
         vdec[r, e["channel_begin"]:e["channel_end"]] = d
-    return spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec
+    return spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec, float(bl_len.max()) / 1e3
 
 
 @pytest.mark.parametrize("S", [32, 64])
 def test_precision_sweep_by_baseline_decile(oracle_mod, idg, S):
-    spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec = _sample(oracle_mod, S)
+    spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec, top_km = _sample(oracle_mod, S)
     N, C, rows = md.shape[0], spec.nchannels, obs.uvw.shape[0]
     sp = spec_for(spec.grid_size, S, C, spec.nstations, obs.aterms.shape[0], spec.image_size)
     for variant in (L.VARIANT_PLAIN, L.VARIANT_BATCHED):
@@ -87,6 +92,8 @@ def test_precision_sweep_by_baseline_decile(oracle_mod, idg, S):
         for name, table, overall in (("grid", gd, overall_g), ("vis", vd, overall_v)):
             line = {"S": S, "variant": "batched" if variant == L.VARIANT_BATCHED else "plain", "output": name,
                     "subgrids": int(N), "overall_rel_rms": overall,
+                    "worst_decile_rel_rms": max(t["rel_rms"] for t in table),
+                    "top_decile_rel_rms": table[-1]["rel_rms"], "longest_baseline_km": round(top_km, 1),
                     "baseline_decile_edges_km": [round(float(x) / 1e3, 1) for x in edges], "deciles": table}
             print("[precision] " + json.dumps(line))
             assert overall <= TOL, line
@@ -103,7 +110,7 @@ def test_channel_recurrence_precision_by_decile(oracle_mod, idg, S):
     per-channel form (whose error is printed beside it)."""
     from idg_gb300 import tuning
 
-    spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec = _sample(oracle_mod, S)
+    spec, obs, md, ext, dec, edges, vis, sub_in, want_g, want_v, covered, vdec, _ = _sample(oracle_mod, S)
     N, C = md.shape[0], spec.nchannels
     steps = np.unique(np.diff(obs.wavenumbers))
     assert steps.size >= 3

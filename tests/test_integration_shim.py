@@ -9,8 +9,7 @@ import subprocess
 import pytest
 
 from conftest import PKG, ROOT
-
-REFERENCE = "/root/reference"
+from oracle import REFERENCE_DIR as REFERENCE
 
 MAIN = r"""
 #include <cstdio>
@@ -34,7 +33,7 @@ int main() {
 """
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference sources not present")
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(REFERENCE), reason="reference sources not present")
 def test_shim_links_into_reference_program(idg, tmp_path):
     from idg_gb300 import _lib
 
