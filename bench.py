@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--serve-jobs", type=int, default=30, help="observations in the serving leg (2 jobs each)")
     ap.add_argument("--serve-rates", default="4,16,32", help="mean arrival rates of the serving leg, jobs/s")
     ap.add_argument("--no-uneven", action="store_true", help="skip the batched-uneven (50,000 mixed subgrids) leg")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="reference arm: skip timing the reference's own CUDA kernels")
     ap.add_argument("--shapes", default="", help="G,D: batched gridder/degridder launch shapes instead of autotuning")
     ap.add_argument("--host-buffers", choices=["auto", "pinned", "hostmem"], default="auto",
                     help="page-locked host buffers of the e2e leg: cudaHostAlloc (pinned), huge-page memory "
@@ -655,6 +657,115 @@ def run_ours(args, rank, world, local_rank):
 # ---------------------------------------------------------------------------
 # reference arm: the reference's CPU algorithm on host cores
 # ---------------------------------------------------------------------------
+def reference_gpu_leg(spec, obs, steps: int = 2) -> dict:
+    """The reference's own CUDA kernels, kernel_gridder_v7 and kernel_degridder_v6,
+    compiled unmodified from its sources for sm_103a (oracle/_ref cubins), on the
+    same workload: one launch each over the whole plan (one CTA of 128 threads
+    per subgrid, as the reference launches them), device time from CUDA events,
+    and their error against the FP64 oracle on 24 subgrids of short, middle
+    and long baselines (the degridder against the oracle with the GPU kernel's
+    own w-offset, (z + 1/2) 2 pi: degridding_benchmark.cu:33)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+
+    why = ref_gpu.available()
+    if why:
+        return {"unavailable": why}
+    import torch
+
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA device"}
+    import oracle as O
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    S, C, G, N = spec.subgrid_size, spec.nchannels, spec.grid_size, spec.n_subgrids
+    nat = obs.aterms.shape[0]
+    md = ops.metadata_tensor(obs.metadata, dev)
+    uvw = torch.from_numpy(obs.uvw).to(dev)
+    k = torch.from_numpy(obs.wavenumbers).to(dev)
+    taper = torch.from_numpy(obs.taper).to(dev)
+    at = torch.from_numpy(np.ascontiguousarray(obs.aterms)).to(dev)
+    vis = D.visibilities(spec, device=dev, seed=spec.seed)
+    vout = torch.empty_like(vis)
+    sub = torch.empty((N, 4, S, S), dtype=torch.complex64, device=dev)
+    torch.cuda.synchronize()
+    try:
+        ref_gpu.RefKernels.check_plan(obs.metadata, spec.n_rows, spec.nstations, nat, S, degridder=True)
+    except ValueError as e:
+        return {"unavailable": f"outside the reference kernels' safe limits: {e}"}
+    K = ref_gpu.RefKernels()
+    stream = torch.cuda.current_stream(dev)
+    h = stream.cuda_stream
+    common = dict(nr_rows=spec.n_rows, nr_aterms=nat, grid_size=G, subgrid_size=S, image_size=spec.image_size,
+                  nr_channels=C, nr_stations=spec.nstations, wavenumbers=k.data_ptr(), spheroidal=taper.data_ptr(),
+                  aterms=at.data_ptr(), d_metadata=md.data_ptr(), stream=h, checked=True)
+
+    def grid():
+        K.gridder(obs.metadata, uvw=uvw.data_ptr(), visibilities=vis.data_ptr(), subgrids=sub.data_ptr(), **common)
+
+    def degrid():
+        K.degridder(obs.metadata, uvw=uvw.data_ptr(), visibilities=vout.data_ptr(), subgrids=sub.data_ptr(), **common)
+
+    grid()
+    degrid()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    g_ms = d_ms = 0.0
+    for _ in range(steps):
+        ev[0].record(stream)
+        grid()
+        ev[1].record(stream)
+        degrid()
+        ev[2].record(stream)
+        ev[2].synchronize()
+        g_ms += ev[0].elapsed_time(ev[1]) / steps
+        d_ms += ev[1].elapsed_time(ev[2]) / steps
+    del vis, vout, sub
+    torch.cuda.empty_cache()
+
+    # error against the FP64 oracle: the first subgrid of 8 short, 8 middle and 8 long baselines
+    bl_len = np.linalg.norm(obs.uvw[:: spec.ntimesteps, :2], axis=1)
+    order = np.argsort(bl_len)
+    pick_bl = np.concatenate([order[:8], order[len(order) // 2: len(order) // 2 + 8], order[-8:]])
+    smd = obs.metadata[pick_bl * spec.subgrids_per_baseline].copy()
+    rows = np.concatenate([np.arange(m["time_offset"], m["time_offset"] + m["nr_timesteps"]) for m in smd])
+    smd["time_offset"] = np.arange(len(smd)) * spec.timesteps_per_subgrid
+    suvw = np.ascontiguousarray(obs.uvw[rows])
+    rng = np.random.default_rng(spec.seed + 77)
+    svis = (rng.standard_normal((len(rows), C, 4)) + 1j * rng.standard_normal((len(rows), C, 4))).astype(np.complex64)
+    ssub = (rng.standard_normal((len(smd), 4, S, S)) + 1j * rng.standard_normal((len(smd), 4, S, S))).astype(np.complex64)
+    d_md, d_uvw = ops.metadata_tensor(smd, dev), torch.from_numpy(suvw).to(dev)
+    d_vis, d_sub = torch.from_numpy(svis).to(dev), torch.from_numpy(ssub).to(dev)
+    g_out = torch.empty_like(d_sub)
+    v_out = torch.empty_like(d_vis)
+    sc = dict(common, nr_rows=len(rows), d_metadata=d_md.data_ptr(), checked=False)
+    K.gridder(smd, uvw=d_uvw.data_ptr(), visibilities=d_vis.data_ptr(), subgrids=g_out.data_ptr(), **sc)
+    K.degridder(smd, uvw=d_uvw.data_ptr(), visibilities=v_out.data_ptr(), subgrids=d_sub.data_ptr(), **sc)
+    torch.cuda.synchronize()
+    K.close()
+    prm = O.params(G, S, C, spec.nstations, len(smd), spec.image_size)
+    want_g = O.gridder(prm, suvw, obs.wavenumbers, svis, obs.taper, obs.aterms, smd)
+    prm_d = O.params(G, S, C, spec.nstations, len(smd), spec.image_size, 1.0)  # w-offset pi n, as the kernel
+    want_v = O.degridder(prm_d, suvw, obs.wavenumbers, ssub, obs.taper, obs.aterms, smd, len(rows),
+                         aterm_mode=O.ATERM_ADJOINT)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    nvis = spec.n_visibilities
+    return {
+        "value": nvis / ((g_ms + d_ms) * 1e-3) / 1e6,
+        "unit": "Mvis/s",
+        "gridder_ms": g_ms,
+        "degridder_ms": d_ms,
+        "steps": steps,
+        "kernels": "kernel_gridder_v7 + kernel_degridder_v6 (gridding/src/gridding_benchmark.cu, "
+                   "degridding_benchmark.cu) compiled unmodified for sm_103a, one CTA of 128 threads per subgrid",
+        "rel_rms_vs_fp64": {"gridder": rel(g_out.cpu().numpy(), want_g), "degridder": rel(v_out.cpu().numpy(), want_v),
+                            "sample": "first subgrid of 8 short, 8 middle and 8 long baselines"},
+    }
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -692,6 +803,7 @@ def run_reference(args, rank, world):
         "config": config_block(spec, args.workload, {"parallelism": "host cores"}),
         "cpu_baseline": last,
         "e2e": {"value": value, "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_gpu": reference_gpu_leg(spec, obs) if not args.no_ref_gpu else None,
     }
 
 

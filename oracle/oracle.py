@@ -16,6 +16,7 @@ from __future__ import annotations
 import ctypes
 import os
 import re
+import shutil
 import subprocess
 
 import numpy as np
@@ -23,6 +24,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libidg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libidgref.so")
+REF_GRIDDER_CUBIN = os.path.join(HERE, "_ref", "ref_gridder.cubin")
+REF_DEGRIDDER_CUBIN = os.path.join(HERE, "_ref", "ref_degridder.cubin")
 
 
 def _reference_dir() -> str:
@@ -99,11 +102,18 @@ def build(with_ref: bool | None = None) -> None:
         ref_src = [os.path.join(g, "src", f) for f in ("gridding_benchmark.cpp", "degridding_benchmark.cpp",
                                                         "gridding_initialization.cpp")]
         bridge = os.path.join(HERE, "ref_bridge.cpp")
+        inc = ["-I" + os.path.join(g, "inc"), "-I" + os.path.join(REFERENCE_DIR, "benchmarks-common", "inc")]
         if _stale(REF_SO, [bridge, *ref_src]):
             os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
-            subprocess.run(["g++", "-std=c++17", *_FLAGS, "-DENABLE_OMP", "-DENABLE_CPU=1", "-w",
-                            "-I" + os.path.join(g, "inc"), "-I" + os.path.join(REFERENCE_DIR, "benchmarks-common", "inc"),
+            subprocess.run(["g++", "-std=c++17", *_FLAGS, "-DENABLE_OMP", "-DENABLE_CPU=1", "-w", *inc,
                             "-o", REF_SO, bridge, *ref_src, "-lm"], check=True)
+        # the reference's GPU kernels, device code only (same command as the Makefile's)
+        for cubin, src in ((REF_GRIDDER_CUBIN, "gridding_benchmark.cu"), (REF_DEGRIDDER_CUBIN, "degridding_benchmark.cu")):
+            cu = os.path.join(g, "src", src)
+            nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+            if os.path.exists(cu) and os.path.exists(nvcc) and _stale(cubin, [cu]):
+                subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-cubin",
+                                "-w", "-DENABLE_GPU=1", *inc, "-o", cubin, cu], check=True)
 
 
 _lib = None

@@ -502,7 +502,62 @@ __device__ __forceinline__ void quad_macs_col(f2 (&acc)[NPAIR][4][2], const f2 (
     }
 }
 
+// Phasors first (PF): the quad's factors X, Y, R of every channel pair are
+// formed before any MAC -- all the pairs' sincos are independent and in
+// flight together -- and the operands are then read one correlation at a
+// time, each used by every channel pair.  Same arithmetic as quad_macs_col.
 template <int NPAIR, bool FAST, typename KP>
+__device__ __forceinline__ void quad_macs_col_pf(f2 (&acc)[NPAIR][4][2], const f2 (&Pc)[NPAIR],
+                                                 const f2 (&Ps)[NPAIR], const KP &kp, float4 g, float B, float Gc,
+                                                 float qv, float qw, uint32_t ops_addr) {
+    const float ty = reduce_2pi_s(B * g.y), tn = reduce_2pi_s(Gc * g.z);
+    const f2 TY = pack2(ty, ty), TN = pack2(tn, tn);
+    const float qy = qv * g.y, qn = qw * g.z;
+    const f2 QY = pack2(qy, qy), QN = pack2(qn, qn);
+    f2 Xr[NPAIR], Xi[NPAIR], Yr[NPAIR], Yi[NPAIR], Rc[NPAIR], Rs[NPAIR];
+#pragma unroll
+    for (int j = 0; j < NPAIR; ++j) {
+        const f2 kj = kappa_pair(kp, j);
+        f2 aq = ffma2(kj, QY, TY), ar = ffma2(kj, QN, TN);
+        if (!FAST) {
+            aq = reduce_2pi(aq);
+            ar = reduce_2pi(ar);
+        }
+        f2 Qc, Qs;
+        sincos_pair(aq, Qc, Qs);
+        sincos_pair(ar, Rc[j], Rs[j]);
+        const f2 nPs = neg2(Ps[j]);
+        const f2 m1 = fmul2(Pc[j], Qc), m3 = fmul2(Pc[j], Qs);
+        Xr[j] = ffma2(nPs, Qs, m1);
+        Yr[j] = ffma2(Ps[j], Qs, m1);
+        Xi[j] = ffma2(Ps[j], Qc, m3);
+        Yi[j] = ffma2(nPs, Qc, m3);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        f2 p[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) lds2(ops_addr + 64 * k + 16 * q, p[2 * q], p[2 * q + 1]);
+#pragma unroll
+        for (int j = 0; j < NPAIR; ++j) {
+            const f2 Zr = ffma2(Yi[j], p[3], ffma2(Yr[j], p[2], ffma2(Xi[j], p[1], fmul2(Xr[j], p[0]))));
+            const f2 Zi = ffma2(Yi[j], p[7], ffma2(Yr[j], p[6], ffma2(Xi[j], p[5], fmul2(Xr[j], p[4]))));
+            acc[j][k][0] = ffma2(Rs[j], Zi, ffma2(Rc[j], Zr, acc[j][k][0]));
+            acc[j][k][1] = ffma2(neg2(Rs[j]), Zr, ffma2(Rc[j], Zi, acc[j][k][1]));
+        }
+    }
+}
+
+template <int NPAIR, bool FAST, bool PF, typename KP>
+__device__ __forceinline__ void quad_col(f2 (&acc)[NPAIR][4][2], const f2 (&Pc)[NPAIR], const f2 (&Ps)[NPAIR],
+                                         const KP &kp, float4 g, float4 c0, float4 c1, uint32_t addr) {
+    if (PF)
+        quad_macs_col_pf<NPAIR, FAST>(acc, Pc, Ps, kp, g, c0.y, c0.z, c1.x, c1.y, addr);
+    else
+        quad_macs_col<NPAIR, FAST>(acc, Pc, Ps, kp, g, c0.y, c0.z, c1.x, c1.y, addr);
+}
+
+template <int NPAIR, bool FAST, bool PF, typename KP>
 __device__ __forceinline__ void column_loop(f2 (&acc)[NPAIR][4][2], const KP &kp, const float4 *geo, float4 c0,
                                             float4 c1, uint32_t ops_addr, int part, int nq) {
     f2 Pc[NPAIR], Ps[NPAIR];
@@ -513,13 +568,33 @@ __device__ __forceinline__ void column_loop(f2 (&acc)[NPAIR][4][2], const KP &kp
             cur = g.x;
             column_factors<NPAIR, FAST>(Pc, Ps, kp, g.x, c0.x, c0.w);
         }
-        quad_macs_col<NPAIR, FAST>(acc, Pc, Ps, kp, g, c0.y, c0.z, c1.x, c1.y, ops_addr + kQuadStride * (uint32_t)i);
+        quad_col<NPAIR, FAST, PF>(acc, Pc, Ps, kp, g, c0, c1, ops_addr + kQuadStride * (uint32_t)i);
+    }
+}
+
+// Column runs of known length (RUN > 0): when every column of the batch holds
+// kLanes * RUN quads and the batch starts on a column, a lane's quads come in
+// runs of RUN down one column; P is formed once per run and the run's quads
+// are one straight-line block (no per-quad test of hx).
+template <int NPAIR, bool FAST, bool PF, int RUN, typename KP>
+__device__ __forceinline__ void column_loop_runs(f2 (&acc)[NPAIR][4][2], const KP &kp, const float4 *geo, float4 c0,
+                                                 float4 c1, uint32_t ops_addr, int part, int nq) {
+    f2 Pc[NPAIR], Ps[NPAIR];
+    for (int i0 = part; i0 < nq; i0 += kLanes * RUN) {
+        column_factors<NPAIR, FAST>(Pc, Ps, kp, geo[i0].x, c0.x, c0.w);
+#pragma unroll
+        for (int u = 0; u < RUN; ++u) {
+            const int i = i0 + kLanes * u;
+            quad_col<NPAIR, FAST, PF>(acc, Pc, Ps, kp, geo[i], c0, c1, ops_addr + kQuadStride * (uint32_t)i);
+        }
     }
 }
 
 // COL: the column form (column_loop); otherwise quads row by row.
-template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false, bool COL = false>
-__global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) {
+// RUN > 0: the column form's runs of RUN quads as straight-line blocks, where
+// the batch's columns hold exactly kLanes * RUN quads.  PF: phasors first.
+template <int NT, int QB, int CB, int UNR, bool KSM, bool COL, int RUN, bool PF>
+__device__ __forceinline__ void degridder_quad_body(const KernelArgs &a) {
     constexpr int kT = NT, kCB = CB, kNP = CB / 2;
     static_assert(CB == 4 || CB == 8, "channel groups of 4 or 8");
     extern __shared__ __align__(16) unsigned char smem[];
@@ -632,11 +707,19 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
 #pragma unroll
                         for (int k = 0; k < 4; ++k) acc[j][k][0] = acc[j][k][1] = 0ull;
                     const float *kps = kap + cfirst;
-                    if (COL) {
+                    const bool runs = RUN > 0 && Sh == kLanes * RUN && qb % Sh == 0 && nq % Sh == 0;
+                    if (COL && runs) {
                         if (fast)
-                            column_loop<kNP, true>(acc, kps, geo, c0, c1, ops_addr, part, nq);
+                            column_loop_runs<kNP, true, PF, (RUN > 0 ? RUN : 1)>(acc, kps, geo, c0, c1, ops_addr,
+                                                                                 part, nq);
                         else
-                            column_loop<kNP, false>(acc, kps, geo, c0, c1, ops_addr, part, nq);
+                            column_loop_runs<kNP, false, PF, (RUN > 0 ? RUN : 1)>(acc, kps, geo, c0, c1, ops_addr,
+                                                                                  part, nq);
+                    } else if (COL) {
+                        if (fast)
+                            column_loop<kNP, true, PF>(acc, kps, geo, c0, c1, ops_addr, part, nq);
+                        else
+                            column_loop<kNP, false, PF>(acc, kps, geo, c0, c1, ops_addr, part, nq);
                     } else if (fast) {
 #pragma unroll UNR
                         for (int i = part; i < nq; i += kLanes) {
@@ -678,10 +761,27 @@ __global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) 
     }
 }
 
-template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false, bool COL = false>
+// The kernel: register budget from the CTAs per SM (MINB), or, with MAXR > 0,
+// a fixed cap of MAXR registers per thread (for CTA sizes whose budget the
+// compiler rounds down: 96-thread CTAs x 3 per SM may use 224 registers).
+template <int NT, int QB, int MINB, int CB, int UNR, bool KSM, bool COL, int RUN, bool PF>
+__global__ void __launch_bounds__(NT, MINB) degridder_quad_kernel(KernelArgs a) {
+    degridder_quad_body<NT, QB, CB, UNR, KSM, COL, RUN, PF>(a);
+}
+template <int MAXR, int NT, int QB, int CB, int UNR, bool KSM, bool COL, int RUN, bool PF>
+__global__ void __maxnreg__(MAXR) degridder_quad_kernel_r(KernelArgs a) {
+    degridder_quad_body<NT, QB, CB, UNR, KSM, COL, RUN, PF>(a);
+}
+
+template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false, bool COL = false, int RUN = 0, bool PF = false,
+          int MAXR = 0>
 cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
     if (a.S % 2 != 0) return cudaErrorInvalidValue;
-    auto kern = degridder_quad_kernel<NT, QB, MINB, CB, UNR, KSM, COL>;
+    void (*kern)(KernelArgs);
+    if constexpr (MAXR > 0)
+        kern = degridder_quad_kernel_r<MAXR, NT, QB, CB, UNR, KSM, COL, RUN, PF>;
+    else
+        kern = degridder_quad_kernel<NT, QB, MINB, CB, UNR, KSM, COL, RUN, PF>;
     const size_t smem = quad_layout(a.S, a.C, QB).total;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -701,7 +801,7 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int degridder_cp_shapes() { return 18; }
+int degridder_cp_shapes() { return 24; }
 
 // Channel-pair shapes (index within this family):
 //   0: 128 threads, 8-channel groups, 256-pixel batches, 4 CTAs/SM (16 warps)
@@ -722,8 +822,20 @@ int degridder_cp_shapes() { return 18; }
 //  15: shape 13 with the quad loop unrolled by two
 //  16: shape 14 reading each channel pair's kappa from shared memory when used
 //  17: mirror quads in column form (P kept per column run), 2 CTAs/SM
+//  18: shape 17 with the phasors of all channel pairs formed first
+//  19: shape 17 with runs of 4 quads as straight-line blocks (S = 32)
+//  20: shapes 18 and 19 together
+//  21: column form, 96 threads x 3 CTAs/SM (9 warps), 128-quad batches
+//  22: shape 21 with the phasors first
+//  23: shape 17 with runs of 8 quads (S = 64)
 cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
+    case 18: return launch_quad<128, 256, 2, 8, 1, true, true, 0, true>(a, stream);
+    case 19: return launch_quad<128, 256, 2, 8, 1, true, true, 4>(a, stream);
+    case 20: return launch_quad<128, 256, 2, 8, 1, true, true, 4, true>(a, stream);
+    case 21: return launch_quad<96, 128, 3, 8, 1, true, true, 0, false, 224>(a, stream);
+    case 22: return launch_quad<96, 128, 3, 8, 1, true, true, 0, true, 224>(a, stream);
+    case 23: return launch_quad<128, 256, 2, 8, 1, true, true, 8>(a, stream);
     case 13: return launch_quad<128, 256, 2, 8, 1>(a, stream);
     case 14: return launch_quad<128, 256, 3, 8, 1>(a, stream);
     case 15: return launch_quad<128, 256, 2, 8, 2>(a, stream);

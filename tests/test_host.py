@@ -265,7 +265,7 @@ def test_reference_arm_line(idg, monkeypatch):
     bench = _load_bench("bench_under_test3")
     real = bench.cpu_baseline
     monkeypatch.setattr(bench, "cpu_baseline", lambda obs, vis, target_s: real(obs, vis, 0.2))
-    args = argparse.Namespace(workload="config1", steps=2, warmup=1)
+    args = argparse.Namespace(workload="config1", steps=2, warmup=1, no_ref_gpu=False)
     out = bench.run_reference(args, 0, 1)
     json.dumps(out)
     assert out["impl"] == "reference" and out["unit"] == "Mvis/s" and out["value"] > 0
@@ -274,4 +274,6 @@ def test_reference_arm_line(idg, monkeypatch):
     cb = out["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == out["value"] and cb["sample"]
     assert out["config"]["workload"].startswith("config1")
+    # without a GPU (or cubins, or within the kernels' limits) the reference kernels' leg says why
+    assert "unavailable" in out["reference_gpu"]
     assert bench.run_reference(args, 1, 2) is None
