@@ -12,6 +12,10 @@ grid-tile ownership so that most of a rank's subgrids land on its own tiles:
 * ``reduce_grid`` sums the per-rank grids with one all-reduce
   (``torch.distributed``: NCCL between GPUs, gloo on CPU); degridding then
   needs the full grid on every rank, which the all-reduce provides.
+* ``sharded_cycle`` is one imaging cycle on the product kernels: each rank
+  grids its part of the plan into its own grid (gridder -> subgrid FFT ->
+  adder), the grids are summed, and each rank degrids its part from the sum.
+  The all-reduce is the only exchange; no kernel waits on another rank.
 """
 from __future__ import annotations
 
@@ -53,12 +57,62 @@ def partition_plan(metadata: np.ndarray, world_size: int, subgrid_size: int, til
 
 
 def reduce_grid(grid, group=None):
-    """Sum a [W,4,G,G] complex64 grid tensor over all ranks, in place (all-reduce)."""
+    """Sum a [W,4,G,G] complex64 grid tensor over all ranks, in place (all-reduce).
+    A device grid under a gloo process group goes through host memory, after
+    the work queued on the current stream."""
     import torch
     import torch.distributed as dist
 
     if not dist.is_available() or not dist.is_initialized() or dist.get_world_size(group) == 1:
         return grid
+    if grid.is_cuda and dist.get_backend(group) == "gloo":
+        torch.cuda.current_stream(grid.device).synchronize()
+        host = grid.cpu()
+        dist.all_reduce(torch.view_as_real(host), op=dist.ReduceOp.SUM, group=group)
+        grid.copy_(host)
+        return grid
     view = torch.view_as_real(grid) if grid.is_complex() else grid
     dist.all_reduce(view, op=dist.ReduceOp.SUM, group=group)
     return grid
+
+
+def _rank_and_world(group=None) -> tuple[int, int]:
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        return dist.get_rank(group), dist.get_world_size(group)
+    return 0, 1
+
+
+def sharded_cycle(spec, metadata: np.ndarray, uvw, wavenumbers, vis, taper, aterms, grid, vis_out,
+                  ext: np.ndarray | None = None, tile: int = 64, variant: int | None = None, group=None) -> np.ndarray:
+    """One imaging cycle of an observation whose inputs every rank holds (device
+    tensors in the layouts of ``ops``), with its subgrids shared out by
+    ``partition_plan``: this rank grids its subgrids with the CUDA kernels into
+    ``grid`` (zeroed first), the ranks' grids are summed in place
+    (``reduce_grid``), and this rank degrids its subgrids from the summed grid
+    into ``vis_out`` (the rows and channels its subgrids name; other entries
+    are left as they are).  Runs on the current stream.  Returns this rank's
+    subgrid indices into ``metadata``."""
+    import torch
+
+    from . import _lib, ops
+
+    if variant is None:
+        variant = _lib.VARIANT_BATCHED
+    rank, world = _rank_and_world(group)
+    md = np.asarray(metadata, METADATA_DTYPE)
+    mine = partition_plan(md, world, spec.subgrid_size, tile, spec.nr_channels, ext)[rank]
+    dev = grid.device
+    grid.zero_()
+    sub = d_md = d_ext = None
+    if len(mine):
+        d_md = ops.metadata_tensor(md[mine], dev)
+        d_ext = ops.ext_tensor(ext[mine], dev) if ext is not None else None
+        sub = torch.empty((len(mine), 4, spec.subgrid_size, spec.subgrid_size), dtype=torch.complex64, device=dev)
+        ops.grid_visibilities(spec, d_md, uvw, wavenumbers, vis, taper, aterms, sub, grid, variant=variant, ext=d_ext)
+    reduce_grid(grid, group)
+    if len(mine):
+        ops.degrid_visibilities(spec, d_md, uvw, wavenumbers, vis_out, taper, aterms, sub, grid, variant=variant,
+                                ext=d_ext)
+    return mine
