@@ -359,6 +359,8 @@ def run_ours(args, rank, world, local_rank):
     stream.synchronize()
 
     nogrid = gs.__class__(**{**gs.__dict__, "flags": gs.flags | 0x2})  # IDG_FLAG_NO_TAPER
+    # the adder with a fixed summation order, as the plan's cycle runs it
+    bins = ops.TileBins(gs, obs.metadata)
 
     # autotune the batched kernels' launch shapes on a leading sample of the plan
     tune = None
@@ -448,7 +450,7 @@ def run_ours(args, rank, world, local_rank):
         if ev: ev[1].record(stream)
         ops.subgrid_fft(gs, sub, +1, taper, stream=stream)
         if ev: ev[2].record(stream)
-        ops.adder(gs, md, sub, grid, stream=stream)
+        bins.add(sub, grid, stream=stream)
         if ev: ev[3].record(stream)
         # degridding step
         ops.splitter(gs, md, grid, sub, stream=stream)

@@ -183,6 +183,24 @@ IDG_API int idg_subgrid_fft(const idg_params *params, int64_t nr_subgrids, int d
  * swapped.  Entries with z outside [-W, W) are skipped. */
 IDG_API int idg_adder(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
                       const void *subgrids, void *grid, void *stream);
+/* The adder with a fixed summation order.  idg_adder() sums overlapping
+ * footprints with floating-point atomics, so the last bits of the grid change
+ * from run to run.  Bins made once from a plan's HOST metadata (the subgrids
+ * of each 32 x 32-cell grid tile, in subgrid order, cut into chunks of 128)
+ * let idg_adder_binned() add the same subgrids with plain loads and stores in
+ * that order: the grid is the same, bit for bit, on every run.  Same
+ * definition as idg_adder(), mirror rule included.  The bins keep a device
+ * copy of the metadata and room for the partial tiles of tiles with more than
+ * one chunk; idg_tile_bins_info() reports (work items, tiles with several
+ * chunks, partial tiles, their bytes).  Calls with the same bins must not
+ * overlap on the GPU (they share the partial tiles).  No counterpart in the
+ * reference; its upstream adder is not vendored. */
+typedef struct idg_tile_bins idg_tile_bins;
+IDG_API int idg_tile_bins_create(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                                 idg_tile_bins **bins);
+IDG_API int idg_tile_bins_destroy(idg_tile_bins *bins);
+IDG_API int idg_tile_bins_info(const idg_tile_bins *bins, int64_t *sizes);
+IDG_API int idg_adder_binned(const idg_tile_bins *bins, const void *subgrids, void *grid, void *stream);
 /* Splitter: F[s][pol][j][i] = grid[z][pol][y+j][x+i] (0 outside); the
  * adder's mirror rule for -W <= z < 0. */
 IDG_API int idg_splitter(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
@@ -264,8 +282,9 @@ IDG_API int idg_plan_subgrids(const idg_planner_params *params, const float *uvw
 /* ------------------------------------------------------------------ */
 /* A plan keeps a set of subgrids on the device: metadata, channel sidecar, a
  * work list ordering the subgrids longest first (uneven subgrids then finish
- * together in one persistent launch), the plan's own scheduler words and the
- * subgrid work space.  `metadata` and `ext` are HOST arrays, validated and
+ * together in one persistent launch), the plan's own scheduler words, the
+ * subgrid work space and the tile bins of its adder (idg_adder_binned: the
+ * plan's grid is the same bit for bit on every run).  `metadata` and `ext` are HOST arrays, validated and
  * copied at creation.  The steps are those of idg_grid_visibilities /
  * idg_degrid_visibilities.  No counterpart in the reference. */
 typedef struct idg_plan idg_plan;

@@ -7,7 +7,9 @@
 // and check word (so plans on different streams never share scheduler
 // state), and the subgrid work space.  A plan can capture a whole cycle --
 // zero the grid, gridder -> FFT -> adder, splitter -> FFT -> degridder -- into
-// one CUDA graph and replay it with a single launch.
+// one CUDA graph and replay it with a single launch.  The plan's adder sums
+// in a fixed order (tile bins made from the host metadata at creation,
+// idg_tiles.cu), so a plan's grid is the same bit for bit on every run.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -16,6 +18,7 @@
 #include "idg_device.cuh"
 #include "idg_host.h"
 #include "idg_internal.h"
+#include "idg_tiles.h"
 
 struct idg_plan {
     idg_params params{};
@@ -28,6 +31,8 @@ struct idg_plan {
     int *d_work = nullptr;
     unsigned *d_words = nullptr; // [0] gridder counter, [1] degridder counter, [2] check word
     void *d_subgrids = nullptr;
+    void *bins_mem = nullptr; // the adder's tile bins (and their own metadata copy)
+    idg::TileBinsDev bins;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
 };
@@ -46,7 +51,7 @@ void plan_free(idg_plan *p) {
     if (!p) return;
     if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
     if (p->graph) cudaGraphDestroy(p->graph);
-    for (void *q : {(void *)p->d_md, (void *)p->d_ext, (void *)p->d_work, (void *)p->d_words, p->d_subgrids})
+    for (void *q : {(void *)p->d_md, (void *)p->d_ext, (void *)p->d_work, (void *)p->d_words, p->d_subgrids, p->bins_mem})
         if (q) cudaFree(q);
     delete p;
 }
@@ -104,8 +109,8 @@ int grid_step(idg_plan *p, const float *uvw, const float *k, const void *vis, co
     if (e != cudaSuccess) return cuda_fail(e, "plan gridder");
     e = launch_subgrid_fft(reinterpret_cast<float2 *>(p->d_subgrids), p->nr_subgrids, q.subgrid_size, +1, taper, st);
     if (e != cudaSuccess) return cuda_fail(e, "plan subgrid fft");
-    e = launch_adder(p->d_md, p->nr_subgrids, q.subgrid_size, q.grid_size, q.nr_w_planes > 0 ? q.nr_w_planes : 1,
-                     reinterpret_cast<const float2 *>(p->d_subgrids), reinterpret_cast<float2 *>(grid), st);
+    e = launch_binned_adder(p->bins, reinterpret_cast<const float2 *>(p->d_subgrids), reinterpret_cast<float2 *>(grid),
+                            st);
     if (e != cudaSuccess) return cuda_fail(e, "plan adder");
     return IDG_OK;
 }
@@ -161,6 +166,9 @@ IDG_API int idg_plan_create(const idg_params *params, int variant, int64_t nr_su
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
 
+    TileBinsHost bins;
+    if (int rc = bin_tiles(params, nr_subgrids, metadata, &bins)) return rc;
+
     idg_plan *p = new idg_plan;
     p->params = *params;
     p->variant = variant;
@@ -187,6 +195,10 @@ IDG_API int idg_plan_create(const idg_params *params, int variant, int64_t nr_su
     if ((e = cudaMemcpy(p->d_work, order.data(), sizeof(int) * nr_subgrids, cudaMemcpyHostToDevice)) != cudaSuccess)
         return bail(e, "plan work list copy");
     if ((e = cudaMemset(p->d_words, 0, 256)) != cudaSuccess) return bail(e, "plan words clear");
+    if (int rc = upload_tile_bins(bins, nr_subgrids, metadata, &p->bins_mem, &p->bins)) {
+        plan_free(p);
+        return rc;
+    }
     *plan = p;
     return IDG_OK;
 }

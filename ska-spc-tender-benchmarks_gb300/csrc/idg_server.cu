@@ -13,8 +13,12 @@
 // live on the device for the server's lifetime: gridding jobs add into one,
 // degridding jobs read one; a job whose kind differs from the running jobs on
 // the same grid waits for them on the GPU (stream-ordered event waits).  The
-// scheduler polls completion events (never blocks in a CUDA call), records
-// queueing, run and total latency per job, and frees the job's memory.
+// adder sums in a fixed order (tile bins made on the host at submission,
+// idg_tiles.cu), and the adders of gridding jobs on one grid run one after
+// another in admission order, so a grid's contents do not depend on how the
+// jobs overlapped.  The scheduler polls completion (never blocks in a CUDA
+// call), records queueing, run and total latency per job, and frees the job's
+// memory.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -31,6 +35,7 @@
 #include "idg_device.cuh"
 #include "idg_host.h"
 #include "idg_internal.h"
+#include "idg_tiles.h"
 
 using namespace idg;
 using Clock = std::chrono::steady_clock;
@@ -48,6 +53,7 @@ struct Grid {
     int last_op = -1;                  // op of the jobs currently holding the grid
     std::vector<cudaEvent_t> holders;  // their completion events
     int readers = 0;                   // idg_server_grid_read calls copying the grid out
+    cudaEvent_t last_add = nullptr;    // end of the adder of the last gridding job admitted on it
 };
 
 struct Job {
@@ -63,6 +69,8 @@ struct Job {
     void *arena = nullptr;
     cudaEvent_t done = nullptr;
     cudaEvent_t k0 = nullptr, k1 = nullptr; // around the job's kernels (timing events)
+    cudaEvent_t add_done = nullptr;         // gridding jobs: after the adder
+    TileBinsHost bins;                      // gridding jobs: the adder's tile bins
     double dev_start_ms = -1, dev_end_ms = -1; // k0, k1 relative to the server's epoch event
     int status = IDG_OK;
     bool finished = false;
@@ -71,10 +79,10 @@ struct Job {
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct Layout {
-    size_t md, ext, work, words, sub, uvw, k, taper, aterms, vis, total;
+    size_t md, ext, work, words, sub, uvw, k, taper, aterms, vis, entries, items, multi, partials, total;
 };
 
-Layout job_layout(const idg_job &j) {
+Layout job_layout(const idg_job &j, const TileBinsHost *bins = nullptr) {
     const idg_params &p = j.params;
     const size_t N = (size_t)j.nr_subgrids, S = (size_t)p.subgrid_size;
     Layout L;
@@ -89,6 +97,10 @@ Layout job_layout(const idg_job &j) {
     L.taper = off; off += align_up(S * S * 4);
     L.aterms = off; off += align_up((size_t)p.nr_aterms * p.nr_stations * S * S * 32);
     L.vis = off; off += align_up((size_t)j.nr_rows * p.nr_channels * 32);
+    L.entries = off; off += bins ? align_up(sizeof(int) * bins->entries.size()) : 0;
+    L.items = off; off += bins ? align_up(sizeof(TileItem) * bins->items.size()) : 0;
+    L.multi = off; off += bins ? align_up(sizeof(TileMulti) * bins->multi.size()) : 0;
+    L.partials = off; off += bins ? align_up(bins->partial_bytes()) : 0;
     L.total = off;
     return L;
 }
@@ -160,7 +172,8 @@ void idg_server::launch(Job &j) {
     cudaSetDevice(device);
     cudaStream_t st = streams[j.slot];
     const idg_params &p = j.spec.params;
-    const Layout L = job_layout(j.spec);
+    const bool gridding = j.spec.op == IDG_JOB_GRID;
+    const Layout L = job_layout(j.spec, gridding ? &j.bins : nullptr);
     char *base = static_cast<char *>(j.arena);
     auto dp = [&](size_t off) { return static_cast<void *>(base + off); };
     const size_t N = j.md.size();
@@ -179,10 +192,19 @@ void idg_server::launch(Job &j) {
     chk(cudaMemcpyAsync(dp(L.aterms), j.spec.aterms, (size_t)p.nr_aterms * p.nr_stations * S * S * 32,
                         cudaMemcpyHostToDevice, st));
     const size_t b_vis = (size_t)j.spec.nr_rows * p.nr_channels * 32;
-    if (j.spec.op == IDG_JOB_GRID)
+    if (gridding) {
         chk(cudaMemcpyAsync(dp(L.vis), j.spec.vis_in, b_vis, cudaMemcpyHostToDevice, st));
-    else
+        chk(cudaMemcpyAsync(dp(L.entries), j.bins.entries.data(), sizeof(int) * j.bins.entries.size(),
+                            cudaMemcpyHostToDevice, st));
+        if (!j.bins.items.empty())
+            chk(cudaMemcpyAsync(dp(L.items), j.bins.items.data(), sizeof(TileItem) * j.bins.items.size(),
+                                cudaMemcpyHostToDevice, st));
+        if (!j.bins.multi.empty())
+            chk(cudaMemcpyAsync(dp(L.multi), j.bins.multi.data(), sizeof(TileMulti) * j.bins.multi.size(),
+                                cudaMemcpyHostToDevice, st));
+    } else {
         chk(cudaMemsetAsync(dp(L.vis), 0, b_vis, st));
+    }
 
     Grid &g = grids[j.spec.grid_id];
     KernelArgs a{};
@@ -224,8 +246,24 @@ void idg_server::launch(Job &j) {
     if (j.spec.op == IDG_JOB_GRID) {
         chk(launch_gridder(a, variant, p.nr_channels, st));
         chk(launch_subgrid_fft(a.subgrids, (int64_t)N, p.subgrid_size, +1, a.taper, st));
-        chk(launch_adder(a.md, (int64_t)N, p.subgrid_size, p.grid_size, g.planes, a.subgrids,
-                         static_cast<float2 *>(g.dev), st));
+        // adders on one grid in admission order: this one after the previous one
+        if (g.last_add) chk(cudaStreamWaitEvent(st, g.last_add, 0));
+        TileBinsDev v;
+        v.md = a.md;
+        v.entries = static_cast<const int *>(dp(L.entries));
+        v.items = static_cast<const TileItem *>(dp(L.items));
+        v.multi = static_cast<const TileMulti *>(dp(L.multi));
+        v.partials = j.bins.nslots ? static_cast<float2 *>(dp(L.partials)) : nullptr;
+        v.S = j.bins.S;
+        v.G = j.bins.G;
+        v.ntx = j.bins.ntx;
+        v.nitems = (int)j.bins.items.size();
+        v.nmulti = (int)j.bins.multi.size();
+        chk(launch_binned_adder(v, a.subgrids, static_cast<float2 *>(g.dev), st));
+        // the next gridding job's adder waits for this one (for the whole job
+        // when the event could not be made: j.done is recorded below)
+        if (j.add_done) chk(cudaEventRecord(j.add_done, st));
+        g.last_add = j.add_done ? j.add_done : j.done;
     } else {
         chk(launch_splitter(a.md, (int64_t)N, p.subgrid_size, p.grid_size, g.planes,
                             static_cast<const float2 *>(g.dev), a.subgrids, st));
@@ -278,6 +316,10 @@ void idg_server::admit_locked() {
         in_use += j.footprint;
         peak_use = std::max(peak_use, in_use);
         cudaEventCreateWithFlags(&j.done, cudaEventDisableTiming);
+        if (j.spec.op == IDG_JOB_GRID && cudaEventCreateWithFlags(&j.add_done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            j.add_done = nullptr; // the job's end event stands in for it
+        }
         if (cudaEventCreate(&j.k0) != cudaSuccess || cudaEventCreate(&j.k1) != cudaSuccess) {
             cudaGetLastError();
             if (j.k0) cudaEventDestroy(j.k0);
@@ -318,13 +360,19 @@ void idg_server::poll_locked() {
         // plan entries the kernels rejected
         if (j.status == IDG_OK) {
             unsigned st = 0;
-            const Layout L = job_layout(j.spec);
+            const Layout L = job_layout(j.spec, j.spec.op == IDG_JOB_GRID ? &j.bins : nullptr);
             cudaMemcpy(&st, static_cast<char *>(j.arena) + L.words + 8, sizeof st, cudaMemcpyDeviceToHost);
             if (st) j.status = IDG_ERR_DEVICE_CHECK;
         }
         Grid &g = grids[j.spec.grid_id];
         g.holders.erase(std::remove(g.holders.begin(), g.holders.end(), j.done), g.holders.end());
         if (g.holders.empty()) g.last_op = -1;
+        if (g.last_add && (g.last_add == j.add_done || g.last_add == j.done))
+            g.last_add = nullptr; // finished: later adders need not wait for it
+        if (j.add_done) {
+            cudaEventDestroy(j.add_done);
+            j.add_done = nullptr;
+        }
         cudaFreeAsync(j.arena, streams[s]);
         cudaEventDestroy(j.done);
         j.done = nullptr;
@@ -522,7 +570,9 @@ IDG_API int idg_server_submit(idg_server *srv, const idg_job *job, int64_t *job_
     j->work.resize(N);
     std::iota(j->work.begin(), j->work.end(), 0);
     std::stable_sort(j->work.begin(), j->work.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-    j->footprint = job_layout(j->spec).total;
+    if (job->op == IDG_JOB_GRID)
+        if (int rc = bin_tiles(&job->params, N, job->metadata, &j->bins)) return rc;
+    j->footprint = job_layout(j->spec, job->op == IDG_JOB_GRID ? &j->bins : nullptr).total;
     std::lock_guard<std::mutex> lock(srv->mu);
     if (j->footprint > (size_t)srv->cfg.hbm_budget_bytes) {
         ++srv->rejected;

@@ -198,6 +198,10 @@ _SIGNATURES = {
     "idg_subgrid_fft": [ctypes.POINTER(IdgParams), _I64, _I32, _P, _P, _P],
     "idg_adder": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
     "idg_splitter": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
+    "idg_tile_bins_create": [ctypes.POINTER(IdgParams), _I64, _P, ctypes.POINTER(ctypes.c_void_p)],
+    "idg_tile_bins_destroy": [_P],
+    "idg_tile_bins_info": [_P, ctypes.POINTER(ctypes.c_int64)],
+    "idg_adder_binned": [_P, _P, _P, _P],
     "idg_grid_fft": [ctypes.POINTER(IdgParams), _P, _I32, _P, _P],
     "idg_grid_visibilities": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P],
     "idg_degrid_visibilities": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P],

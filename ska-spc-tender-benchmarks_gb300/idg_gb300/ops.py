@@ -144,6 +144,45 @@ def adder(spec: GridSpec, metadata, subgrids, grid, stream=None):
     return grid
 
 
+class TileBins:
+    """The adder with a fixed summation order (idg_tile_bins_* / idg_adder_binned):
+    bins made once from a plan's host metadata; ``add`` sums the plan's
+    subgrids into a grid in the same order on every call, so the grid is
+    reproducible bit for bit."""
+
+    def __init__(self, spec: GridSpec, metadata: np.ndarray):
+        md = np.ascontiguousarray(metadata, dtype=_lib.METADATA_DTYPE)
+        self.spec = spec
+        self.nr_subgrids = md.shape[0]
+        p = spec.to_c()
+        h = ctypes.c_void_p()
+        _lib.call("idg_tile_bins_create", ctypes.byref(p), md.shape[0], ptr(md), ctypes.byref(h))
+        self._h = h
+
+    def info(self) -> dict:
+        v = (ctypes.c_int64 * 4)()
+        _lib.call("idg_tile_bins_info", self._h, v)
+        return {"work_items": v[0], "multi_chunk_tiles": v[1], "partial_tiles": v[2], "partial_bytes": v[3]}
+
+    def add(self, subgrids, grid, stream=None):
+        S, G, W = self.spec.subgrid_size, self.spec.grid_size, self.spec.nr_w_planes
+        _req(subgrids, "subgrids", torch.complex64, (self.nr_subgrids, 4, S, S))
+        _req(grid, "grid", torch.complex64, (W, 4, G, G))
+        _lib.call("idg_adder_binned", self._h, ptr(subgrids), ptr(grid), _stream_handle(stream))
+        return grid
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().idg_tile_bins_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def splitter(spec: GridSpec, metadata, grid, subgrids, stream=None):
     S, G, W = spec.subgrid_size, spec.grid_size, spec.nr_w_planes
     _req(metadata, "metadata", torch.int32)
