@@ -11,9 +11,10 @@
 //    cells of their target plane (a counting sort in subgrid order, so each
 //    tile's list is ascending).  Each list is cut into chunks of at most
 //    kChunk subgrids.
-//  * Pass 1, one CTA per chunk: every thread owns four cells of one column of
-//    the tile (all four correlations) and adds the chunk's subgrids into
-//    registers, in list order.  A tile with one chunk is then added into the
+//  * Pass 1, one CTA per chunk: the chunk's plan entries are staged in shared
+//    memory; every thread owns four cells of one column of the tile (all four
+//    correlations) and adds the chunk's subgrids into registers, in list
+//    order.  A tile with one chunk is then added into the
 //    grid with plain loads and stores -- no other CTA touches it; a tile with
 //    several chunks writes each chunk's sum to a partial tile.
 //  * Pass 2, one CTA per tile with several chunks: grid += partial 0, then
@@ -40,10 +41,22 @@ constexpr int kChunk = 128;     // subgrids per pass-1 work item
 
 __device__ __forceinline__ int swap_pol(int p) { return (p == 1 || p == 2) ? 3 - p : p; }
 
-__global__ void __launch_bounds__(kTile * kWarps, 4)
+// The chunk's plan entries (x, y, z, subgrid) are staged in shared memory
+// first; the entry loop then issues predicated loads (cells outside an entry's
+// footprint load nothing and add zero) takes two entries per step, so that
+// both entries' loads are in flight before either is added.  The adds stay in
+// list order.
+__global__ void __launch_bounds__(kTile * kWarps, 2)
     tile_add_kernel(const TileItem *items, const int *entries, const idg_metadata *md, int S, int G, int ntx,
                     const float2 *subgrids, float2 *grid, float2 *partials) {
+    __shared__ int4 smd[kChunk];
     const TileItem it = items[blockIdx.x];
+    const int n = it.end - it.begin;
+    for (int e = threadIdx.x; e < n; e += kTile * kWarps) {
+        const int s = entries[it.begin + e];
+        const idg_metadata m = md[s];
+        smd[e] = make_int4(m.x, m.y, m.z, s);
+    }
     const int per_plane = ntx * ntx;
     const int plane = it.tile / per_plane, r = it.tile - plane * per_plane, ty = r / ntx, tx = r - ty * ntx;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -54,28 +67,42 @@ __global__ void __launch_bounds__(kTile * kWarps, 4)
     for (int k = 0; k < kRowsPerThread; ++k)
 #pragma unroll
         for (int p = 0; p < 4; ++p) acc[k][p] = make_float2(0.f, 0.f);
+    __syncthreads();
 
-    for (int e = it.begin; e < it.end; ++e) {
-        const int s = entries[e];
-        const idg_metadata m = md[s];
-        const bool mirror = m.z < 0;
-        const int i = mirror ? G - gx - m.x : gx - m.x;
-        if ((unsigned)i >= (unsigned)S || gx >= G) continue;
-        const float2 *src = subgrids + (int64_t)s * 4 * S2 + i;
+    // two entries per step: both entries' loads are issued before either is added
+    for (int e = 0; e < n; e += 2) {
+        float2 v[2][kRowsPerThread][4];
+        bool mir[2];
 #pragma unroll
-        for (int k = 0; k < kRowsPerThread; ++k) {
-            const int gy = ty * kTile + warp + kWarps * k;
-            const int j = mirror ? G - gy - m.y : gy - m.y;
-            if ((unsigned)j >= (unsigned)S || gy >= G) continue;
+        for (int h = 0; h < 2; ++h) {
+            const int4 m = smd[e + h < n ? e + h : e];
+            const bool live = e + h < n;
+            mir[h] = m.z < 0;
+            const int i = mir[h] ? G - gx - m.x : gx - m.x;
+            const bool xin = live && (unsigned)i < (unsigned)S && gx < G;
+            const float2 *src = subgrids + (int64_t)m.w * 4 * S2 + (xin ? i : 0);
 #pragma unroll
-            for (int p = 0; p < 4; ++p) {
-                // grid correlation p takes subgrid correlation p, or its swap when mirrored (conjugated)
-                const int q = mirror ? swap_pol(p) : p;
-                const float2 v = src[q * S2 + (int64_t)j * S];
-                acc[k][p].x += v.x;
-                acc[k][p].y += mirror ? -v.y : v.y;
+            for (int k = 0; k < kRowsPerThread; ++k) {
+                const int gy = ty * kTile + warp + kWarps * k;
+                const int j = mir[h] ? G - gy - m.y : gy - m.y;
+                const bool in = xin && (unsigned)j < (unsigned)S && gy < G;
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    // grid correlation p takes subgrid correlation p, or its swap when mirrored
+                    const int q = mir[h] ? swap_pol(p) : p;
+                    v[h][k][p] = in ? __ldg(src + q * S2 + (int64_t)j * S) : make_float2(0.f, 0.f);
+                }
             }
         }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int k = 0; k < kRowsPerThread; ++k)
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    acc[k][p].x += v[h][k][p].x;
+                    acc[k][p].y += mir[h] ? -v[h][k][p].y : v[h][k][p].y; // mirrored: conjugated
+                }
     }
 
     if (gx >= G) return;
