@@ -133,7 +133,7 @@ def config_block(spec, name, extra=None):
 # ---------------------------------------------------------------------------
 # CPU baseline: the reference's CPU algorithm on a bounded sample
 # ---------------------------------------------------------------------------
-def cpu_baseline(obs, vis_host: np.ndarray, target_s: float):
+def cpu_baseline(obs, vis_host: np.ndarray, target_s: float, build: str = "-O2"):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
@@ -158,11 +158,13 @@ def cpu_baseline(obs, vis_host: np.ndarray, target_s: float):
         vis = np.ascontiguousarray(vis_host[:rows])
         sub = np.zeros((n, 4, S, S), np.complex64)
         t0 = time.perf_counter()
-        O.cpu_gridding_omp(prm, uvw, obs.wavenumbers, vis, obs.taper, np.ascontiguousarray(obs.aterms), md, sub)
+        O.cpu_gridding_omp(prm, uvw, obs.wavenumbers, vis, obs.taper, np.ascontiguousarray(obs.aterms), md, sub,
+                           build=build)
         tg = time.perf_counter() - t0
         out = np.zeros_like(vis)
         t0 = time.perf_counter()
-        O.cpu_degridding_omp(prm, uvw, obs.wavenumbers, sub, obs.taper, np.ascontiguousarray(obs.aterms), md, out)
+        O.cpu_degridding_omp(prm, uvw, obs.wavenumbers, sub, obs.taper, np.ascontiguousarray(obs.aterms), md, out,
+                             build=build)
         td = time.perf_counter() - t0
         return tg, td
 
@@ -179,7 +181,7 @@ def cpu_baseline(obs, vis_host: np.ndarray, target_s: float):
         "kind": "port",
         "sample": f"first {n} of {spec.n_subgrids} subgrids of the same plan ({nvis} visibilities); "
                   f"gridding {tg:.2f} s + degridding {td:.2f} s on {O.omp_threads()} OpenMP threads "
-                  f"(float restatement of the reference's OpenMP CPU launchers, -O2)",
+                  f"(float restatement of the reference's OpenMP CPU launchers, {build})",
     }
 
 
@@ -789,6 +791,11 @@ def run_reference(args, rank, world):
         vals.append(last["value"])
     value = float(np.mean(vals))
     last["value"] = value
+    # the same restatement built as the reference's CMake builds it (-g, no
+    # optimisation) and at -O3, each on a short bounded sample
+    builds = {"-O2": value}
+    for b in ("-O3", "-O0 -g"):
+        builds[b] = cpu_baseline(obs, vis, 2.5, build=b)["value"]
     return {
         "metric": METRIC,
         "impl": "reference",
@@ -804,6 +811,7 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded)",
         "config": config_block(spec, args.workload, {"parallelism": "host cores"}),
         "cpu_baseline": last,
+        "cpu_builds_mvis_per_s": builds,
         "e2e": {"value": value, "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_gpu": reference_gpu_leg(spec, obs) if not args.no_ref_gpu else None,
     }

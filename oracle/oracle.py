@@ -95,6 +95,9 @@ def build(with_ref: bool | None = None) -> None:
     if _stale(ORACLE_SO, src):
         os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
         subprocess.run(["gcc", "-std=gnu11", *_FLAGS, "-o", ORACLE_SO, src[0], "-lm"], check=True)
+    for build_type in BUILD_FLAGS:  # the CPU baseline's other builds, compiled ahead of any timing
+        if build_type != "-O2":
+            _compile_variant(build_type)
     if with_ref is None:
         with_ref = bool(REFERENCE_DIR) and os.path.isdir(REFERENCE_DIR)
     if with_ref:
@@ -118,6 +121,33 @@ def build(with_ref: bool | None = None) -> None:
 
 _lib = None
 _ref = None
+_variants: dict = {}
+
+# Builds of the float restatement for the CPU baseline: the oracle's own -O2,
+# -O3, and -O0 -g, the reference CMake's build type (gridding/CMakeLists.txt:37
+# sets -g and no optimisation level).  -march/-mcpu=native is not used: the
+# same flags must build on x86-64 and aarch64 hosts.
+BUILD_FLAGS = {"-O2": ["-O2"], "-O3": ["-O3"], "-O0 -g": ["-O0", "-g"]}
+
+
+def variant_lib(build: str = "-O2") -> ctypes.CDLL:
+    """The oracle library compiled with one of BUILD_FLAGS (built on first use)."""
+    if build == "-O2":
+        return lib()
+    if build not in _variants:
+        _variants[build] = ctypes.CDLL(_compile_variant(build))
+    return _variants[build]
+
+
+def _compile_variant(build: str) -> str:
+    tag = build.replace(" ", "").replace("-", "")
+    path = os.path.join(HERE, "_build", f"libidg_oracle_{tag}.so")
+    src = os.path.join(HERE, "idg_oracle.c")
+    if _stale(path, [src, os.path.join(HERE, "idg_oracle.h")]):
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        flags = [f for f in _FLAGS if f != "-O2"] + BUILD_FLAGS[build]
+        subprocess.run(["gcc", "-std=gnu11", *flags, "-o", path, src, "-lm"], check=True)
+    return path
 
 
 def lib() -> ctypes.CDLL:
@@ -229,15 +259,15 @@ def omp_threads() -> int:
     return int(lib().oracle_omp_max_threads())
 
 
-def cpu_gridding_omp(prm, uvw, wavenumbers, vis, spheroidal, aterms, metadata, out):
+def cpu_gridding_omp(prm, uvw, wavenumbers, vis, spheroidal, aterms, metadata, out, build: str = "-O2"):
     """Timed CPU baseline (float restatement of the reference's OMP launcher). Writes into `out`."""
-    return lib().oracle_cpu_gridding_omp(ctypes.byref(prm), _p(uvw), _p(wavenumbers), _p(vis), _p(spheroidal),
-                                         _p(aterms), _p(metadata), _p(out))
+    return variant_lib(build).oracle_cpu_gridding_omp(ctypes.byref(prm), _p(uvw), _p(wavenumbers), _p(vis),
+                                                      _p(spheroidal), _p(aterms), _p(metadata), _p(out))
 
 
-def cpu_degridding_omp(prm, uvw, wavenumbers, subgrids, spheroidal, aterms, metadata, out):
-    return lib().oracle_cpu_degridding_omp(ctypes.byref(prm), _p(uvw), _p(wavenumbers), _p(subgrids), _p(spheroidal),
-                                           _p(aterms), _p(metadata), _p(out))
+def cpu_degridding_omp(prm, uvw, wavenumbers, subgrids, spheroidal, aterms, metadata, out, build: str = "-O2"):
+    return variant_lib(build).oracle_cpu_degridding_omp(ctypes.byref(prm), _p(uvw), _p(wavenumbers), _p(subgrids),
+                                                        _p(spheroidal), _p(aterms), _p(metadata), _p(out))
 
 
 # ---------------------------------------------------------------------------

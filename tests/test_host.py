@@ -264,7 +264,7 @@ def test_reference_arm_line(idg, monkeypatch):
 
     bench = _load_bench("bench_under_test3")
     real = bench.cpu_baseline
-    monkeypatch.setattr(bench, "cpu_baseline", lambda obs, vis, target_s: real(obs, vis, 0.2))
+    monkeypatch.setattr(bench, "cpu_baseline", lambda obs, vis, target_s, build="-O2": real(obs, vis, 0.2, build))
     args = argparse.Namespace(workload="config1", steps=2, warmup=1, no_ref_gpu=False)
     out = bench.run_reference(args, 0, 1)
     json.dumps(out)
@@ -274,6 +274,9 @@ def test_reference_arm_line(idg, monkeypatch):
     cb = out["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == out["value"] and cb["sample"]
     assert out["config"]["workload"].startswith("config1")
+    # the port as the reference's CMake builds it (-g, no optimisation) and at -O3, beside -O2
+    assert set(out["cpu_builds_mvis_per_s"]) == {"-O2", "-O3", "-O0 -g"}
+    assert all(v > 0 for v in out["cpu_builds_mvis_per_s"].values())
     # without a GPU (or cubins, or within the kernels' limits) the reference kernels' leg says why
     assert "unavailable" in out["reference_gpu"]
     assert bench.run_reference(args, 1, 2) is None
