@@ -65,6 +65,24 @@ __host__ __device__ inline Layout layout(int S, int C, int tile_vis) {
     return L;
 }
 
+// The mirror-quad kernel's own layout: raw and expanded visibilities (4
+// duplicated operand pairs, 64 B, per visibility), coefficients and kappa; its
+// quad geometry follows `total` (the pixel-pair geometry and channel chains
+// of the layout above are not used).
+struct QuadLayout {
+    size_t raw, vexp, coef, kappa, total;
+};
+__host__ __device__ inline QuadLayout quad_layout(int C, int tile_vis) {
+    QuadLayout L;
+    size_t off = 64;                                   // SmemHead
+    L.raw = off;  off += (size_t)tile_vis * 32;
+    L.vexp = off; off += (size_t)tile_vis * 64;
+    L.coef = off; off += (size_t)kMaxTT * 48;
+    L.kappa = off; off += (size_t)C * 8;
+    L.total = (off + 15) & ~size_t(15);
+    return L;
+}
+
 __device__ __forceinline__ f2 dup(float v) { return pack2(v, v); }
 __device__ __forceinline__ f2 neg2(f2 v) { return v ^ 0x8000000080000000ull; }
 
@@ -692,7 +710,7 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
     // quad g of a pass has x column g mod Sh; with NT a multiple of Sh every quad
     // of a thread (offsets multiples of NT) is in the thread's column
     const bool shared_x = NT % Sh == 0;
-    const Layout L = layout(S, a.C, TV);
+    const QuadLayout L = quad_layout(a.C, TV);
     SmemHead *head = reinterpret_cast<SmemHead *>(smem);
     float4 *raw = reinterpret_cast<float4 *>(smem + L.raw);
     float4 *vq = reinterpret_cast<float4 *>(smem + L.vexp);
@@ -884,6 +902,8 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
 //  20: mirror quads, 64 threads x 4 quads, 4 CTAs/SM (8 warps), unrolled by two (whole passes for S = 32)
 //  21: mirror quads, 128 threads x 4 quads, 2 CTAs/SM (8 warps), unrolled by two (whole passes for S = 64)
 //  22: shape 20 with the channel loop unrolled by four
+//  23: shape 22 with 384-visibility tiles (fewer stages per subgrid)
+//  24: shape 22 with 512-visibility tiles
 // load_only: only make sure the kernel is loaded into the current context
 // (under lazy module loading a kernel is otherwise loaded, which takes device
 // memory, at its first launch).
@@ -919,7 +939,7 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream, bool load_only
         return cudaFuncGetAttributes(&fa, kern);
     }
     if (a.S % 2 != 0) return cudaErrorInvalidValue;
-    const size_t smem = layout(a.S, a.C, TV).total + (size_t)NT * GP * 3 * sizeof(f2); // + quad geometry
+    const size_t smem = quad_layout(a.C, TV).total + (size_t)NT * GP * 3 * sizeof(f2); // + quad geometry
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -938,7 +958,7 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream, bool load_only
 
 } // namespace
 
-int gridder_fast_shapes() { return 23; }
+int gridder_fast_shapes() { return 25; }
 
 namespace {
 cudaError_t dispatch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int shape, bool load_only) {
@@ -965,6 +985,8 @@ cudaError_t dispatch_gridder_fast(const KernelArgs &a, cudaStream_t stream, int 
     case 20: return launch_quad<64, 2, 256, 4, 2>(a, stream, load_only);
     case 21: return launch_quad<128, 2, 256, 2, 2>(a, stream, load_only);
     case 22: return launch_quad<64, 2, 256, 4, 4>(a, stream, load_only);
+    case 23: return launch_quad<64, 2, 384, 4, 4>(a, stream, load_only);
+    case 24: return launch_quad<64, 2, 512, 4, 4>(a, stream, load_only);
     default: return launch_shape<128, 4, 256, 3, 0>(a, stream, load_only);
     }
 }
