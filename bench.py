@@ -398,7 +398,7 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_e2e:
         vis_host, out_host, host_rec = e2e_host_buffers(args.host_buffers, (e2e_rows,) + tuple(vis.shape[1:]),
                                                         vis[:e2e_rows], vis_out[:e2e_rows], stream)
-        chunk = max(1, e2e_n // 32)
+        chunk = -1  # IDG_CHUNKS_AUTO: gridding chunks growing, degridding chunks shrinking
         aterms_np = hostmem.pinned_copy(obs.aterms)
         md_e2e = hostmem.pinned_copy(obs.metadata[:e2e_n])
         uvw_e2e = hostmem.pinned_copy(obs.uvw[:e2e_rows])
@@ -430,7 +430,7 @@ def run_ours(args, rank, world, local_rank):
                "d2h_gbs_steps": [round(t["d2h_vis_bytes"] / (t["d2h_vis_ms"] * 1e-3) / 1e9, 1) for t in totals],
                "host_buffers_gb": round((vis_host.nbytes + out_host.nbytes + sum(x.nbytes for x in small)) / 1e9, 2),
                "subgrids": e2e_n,
-               "chunks": (e2e_n + chunk - 1) // chunk,
+               "chunks": {"gridding": int(totals[-1]["grid_chunks"]), "degridding": int(totals[-1]["degrid_chunks"])},
                "gridding_ms": float(np.mean([t["gridding_ms"] for t in totals])),
                "degridding_ms": float(np.mean([t["degridding_ms"] for t in totals])),
                "steps_ms": [round(x, 1) for x in steps_ms],

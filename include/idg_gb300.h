@@ -423,15 +423,25 @@ typedef struct idg_cycle_timing {
     double d2h_vis_ms;
     int64_t h2d_vis_bytes;
     int64_t d2h_vis_bytes;
+    int64_t grid_chunks;   /* chunks of the gridding phase */
+    int64_t degrid_chunks; /* chunks of the degridding phase */
 } idg_cycle_timing;
+
+/* chunk_subgrids of idg_imaging_cycle: chunks sized for the copy pipeline */
+#define IDG_CHUNKS_AUTO (-1)
 
 /* One imaging cycle on HOST buffers: copies the plan, uvw, wavenumbers,
  * taper, A-terms and input visibilities in, grids them into a zeroed grid,
  * degrids the grid back into predicted visibilities and copies those out
  * (and the grid, if `grid_out` is not NULL).  Visibility copies are cut into
- * `chunk_subgrids`-subgrid chunks on their own streams so that transfers
- * overlap the kernels (the plan's rows must then be in chunk order; otherwise
- * the cycle runs as one chunk).  Device buffers are kept between calls of
+ * chunks on their own streams so that transfers overlap the kernels (the
+ * plan's rows must then be in chunk order; otherwise the cycle runs as one
+ * chunk).  chunk_subgrids > 0: chunks of that many subgrids; IDG_CHUNKS_AUTO:
+ * eight chunks per phase whose sizes double from chunk to chunk while
+ * gridding (the first copy in is small, so the kernels start early, and each
+ * later copy finishes while the previous chunk is gridded) and halve while
+ * degridding (the last copy out is small), at least 1024 subgrids each;
+ * 0: one chunk.  uvw rows travel with their chunk.  Device buffers are kept between calls of
  * the same sizes and freed by idg_release_buffers().  Pinned host buffers
  * give full copy bandwidth.  The cycle clears the device check word (see
  * idg_device_status) before its first kernel and returns IDG_ERR_DEVICE_CHECK

@@ -47,6 +47,57 @@ struct CycleBuffers {
 std::mutex g_cycle_mutex;
 CycleBuffers g_cycle;
 
+// A chunk of the host-buffer cycle: subgrids [s0, s1) and the rows [r0, r1)
+// they name.
+struct Chunk {
+    int64_t s0, s1, r0, r1;
+};
+
+// Subgrid boundaries 0 = b0 < b1 < ... = n.  chunk > 0: equal chunks of that
+// many subgrids; IDG_CHUNKS_AUTO: eight chunks whose sizes double from one to
+// the next (`growing`) or halve (otherwise), chunks under kMinChunk subgrids
+// merged into their neighbour; anything else: one chunk.
+constexpr int64_t kMinChunk = 1024;
+std::vector<int64_t> chunk_bounds(int64_t n, int64_t chunk, bool growing) {
+    std::vector<int64_t> b{0};
+    if (chunk == IDG_CHUNKS_AUTO) {
+        const int k = 8;
+        const double total = (double)((1 << k) - 1);
+        double acc = 0;
+        for (int i = 0; i < k; ++i) {
+            acc += (double)(1 << (growing ? i : k - 1 - i));
+            const int64_t e = i == k - 1 ? n : (int64_t)(n * acc / total + 0.5);
+            if (e - b.back() >= kMinChunk) b.push_back(e);
+        }
+        if (b.size() == 1) b.push_back(n);
+        b.back() = n; // the last chunk takes what the merges left
+        return b;
+    }
+    if (chunk < 1 || chunk >= n) chunk = n;
+    for (int64_t s = chunk; s < n; s += chunk) b.push_back(s);
+    b.push_back(n);
+    return b;
+}
+
+// The chunks of `bounds` with their row ranges; false when a chunk's rows
+// start before the previous chunk's end (the plan is not in row order).
+bool make_chunks(const std::vector<int64_t> &bounds, const std::vector<int64_t> &row0,
+                 const std::vector<int64_t> &row1, std::vector<Chunk> *out) {
+    out->clear();
+    int64_t prev_end = 0;
+    for (size_t i = 0; i + 1 < bounds.size(); ++i) {
+        Chunk c{bounds[i], bounds[i + 1], INT64_MAX, 0};
+        for (int64_t s = c.s0; s < c.s1; ++s) {
+            c.r0 = std::min(c.r0, row0[s]);
+            c.r1 = std::max(c.r1, row1[s]);
+        }
+        if (c.r0 < prev_end) return false;
+        prev_end = c.r1;
+        out->push_back(c);
+    }
+    return true;
+}
+
 int ensure(void **p, size_t *have, size_t want) {
     if (want == 0) want = 16;
     if (*p && *have >= want) return IDG_OK;
@@ -112,37 +163,25 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     const int64_t S = params->subgrid_size, C = params->nr_channels, G = params->grid_size;
     const int64_t W = params->nr_w_planes > 0 ? params->nr_w_planes : 1;
 
-    // chunk row ranges; rows must advance chunk by chunk to overlap copies
-    if (chunk_subgrids < 1 || chunk_subgrids > nr_subgrids) chunk_subgrids = nr_subgrids;
+    // rows of every entry, checked; then the chunks of each phase (rows must
+    // advance chunk by chunk for the copies to overlap the kernels)
     const int bo1 = metadata[0].baseline_offset;
-    std::vector<int64_t> c_begin, c_rows0, c_rows1;
-    int64_t prev_end = 0;
-    bool ordered = true;
-    for (int64_t s0 = 0; s0 < nr_subgrids; s0 += chunk_subgrids) {
-        const int64_t s1 = std::min(nr_subgrids, s0 + chunk_subgrids);
-        int64_t r0 = INT64_MAX, r1 = 0;
-        for (int64_t s = s0; s < s1; ++s) {
-            const idg_metadata &m = metadata[s];
-            const int64_t a = (int64_t)(m.baseline_offset - bo1) + m.time_offset;
-            if (a < 0 || m.nr_timesteps < 0 || a + m.nr_timesteps > nr_rows)
-                return fail(IDG_ERR_INVALID_ARGUMENT, "plan entry %lld names rows outside [0, %lld)", (long long)s,
-                            (long long)nr_rows);
-            r0 = std::min(r0, a);
-            r1 = std::max(r1, a + m.nr_timesteps);
-        }
-        if (r0 < prev_end) ordered = false;
-        prev_end = r1;
-        c_begin.push_back(s0);
-        c_rows0.push_back(r0);
-        c_rows1.push_back(r1);
+    std::vector<int64_t> row0(nr_subgrids), row1(nr_subgrids);
+    for (int64_t s = 0; s < nr_subgrids; ++s) {
+        const idg_metadata &m = metadata[s];
+        const int64_t a = (int64_t)(m.baseline_offset - bo1) + m.time_offset;
+        if (a < 0 || m.nr_timesteps < 0 || a + m.nr_timesteps > nr_rows)
+            return fail(IDG_ERR_INVALID_ARGUMENT, "plan entry %lld names rows outside [0, %lld)", (long long)s,
+                        (long long)nr_rows);
+        row0[s] = a;
+        row1[s] = a + m.nr_timesteps;
     }
-    if (!ordered) {
-        c_begin.assign(1, 0);
-        c_rows0.assign(1, 0);
-        c_rows1.assign(1, nr_rows);
+    std::vector<Chunk> gch, dch;
+    if (!make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, true), row0, row1, &gch) ||
+        !make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, false), row0, row1, &dch)) {
+        gch.assign(1, Chunk{0, nr_subgrids, 0, nr_rows});
+        dch = gch;
     }
-    c_begin.push_back(nr_subgrids);
-    const size_t nchunks = c_rows0.size();
 
     std::lock_guard<std::mutex> lock(g_cycle_mutex);
     CycleBuffers &B = g_cycle;
@@ -196,9 +235,10 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     cudaEvent_t h2d_v0, h2d_v1;
     if (int rc = new_event(&h2d_v0, true)) return rc;
     if (int rc = new_event(&h2d_v1, true)) return rc;
-    std::vector<cudaEvent_t> h2d_done(nchunks), deg_done(nchunks), d2h_b(nchunks), d2h_e(nchunks);
-    for (size_t i = 0; i < nchunks; ++i) {
+    std::vector<cudaEvent_t> h2d_done(gch.size()), deg_done(dch.size()), d2h_b(dch.size()), d2h_e(dch.size());
+    for (size_t i = 0; i < gch.size(); ++i)
         if (int rc = new_event(&h2d_done[i], false)) return rc;
+    for (size_t i = 0; i < dch.size(); ++i) {
         if (int rc = new_event(&deg_done[i], false)) return rc;
         if (int rc = new_event(&d2h_b[i], true)) return rc;
         if (int rc = new_event(&d2h_e[i], true)) return rc;
@@ -222,17 +262,26 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     IDG_CUDA(cudaMemsetAsync(w.status, 0, sizeof(unsigned), B.s_compute));
     int64_t launches = 0, h2d = 0, d2h = 0, h2d_vis = 0, d2h_vis = 0;
     IDG_CUDA(cudaEventRecord(t_start, B.s_h2d));
-    // constants first (small), then visibility chunks
+    // constants first (small), then each chunk's uvw rows and visibilities
     IDG_CUDA(cudaMemcpyAsync(B.md, metadata, b_md, cudaMemcpyHostToDevice, B.s_h2d));
-    IDG_CUDA(cudaMemcpyAsync(B.uvw, uvw, b_uvw, cudaMemcpyHostToDevice, B.s_h2d));
     IDG_CUDA(cudaMemcpyAsync(B.k, wavenumbers, b_k, cudaMemcpyHostToDevice, B.s_h2d));
     IDG_CUDA(cudaMemcpyAsync(B.taper, spheroidal, b_taper, cudaMemcpyHostToDevice, B.s_h2d));
     IDG_CUDA(cudaMemcpyAsync(B.aterms, aterms, b_aterms, cudaMemcpyHostToDevice, B.s_h2d));
-    h2d += b_md + b_uvw + b_k + b_taper + b_aterms;
+    h2d += b_md + b_k + b_taper + b_aterms;
     IDG_CUDA(cudaEventRecord(consts_in, B.s_h2d));
     IDG_CUDA(cudaEventRecord(h2d_v0, B.s_h2d));
-    for (size_t i = 0; i < nchunks; ++i) {
-        const size_t off = (size_t)c_rows0[i] * C * 32, bytes = (size_t)(c_rows1[i] - c_rows0[i]) * C * 32;
+    for (size_t i = 0; i < gch.size(); ++i) {
+        const Chunk &c = gch[i];
+        // uvw: this chunk's rows, with any rows before them that no chunk names
+        // (and, for the last chunk, the rows after it)
+        const int64_t u0 = i == 0 ? 0 : gch[i - 1].r1, u1 = i + 1 == gch.size() ? nr_rows : c.r1;
+        if (u1 > u0) {
+            IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.uvw) + (size_t)u0 * 12,
+                                     reinterpret_cast<const char *>(uvw) + (size_t)u0 * 12, (size_t)(u1 - u0) * 12,
+                                     cudaMemcpyHostToDevice, B.s_h2d));
+            h2d += (u1 - u0) * 12;
+        }
+        const size_t off = (size_t)c.r0 * C * 32, bytes = (size_t)(c.r1 - c.r0) * C * 32;
         IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.vis_in) + off, static_cast<const char *>(visibilities_in) + off,
                                  bytes, cudaMemcpyHostToDevice, B.s_h2d));
         h2d += bytes;
@@ -246,9 +295,9 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     IDG_CUDA(cudaMemsetAsync(B.grid, 0, b_grid, B.s_compute));
     IDG_CUDA(cudaEventRecord(t_grid0, B.s_compute));
     const idg_metadata *d_md = static_cast<const idg_metadata *>(B.md);
-    for (size_t i = 0; i < nchunks; ++i) {
+    for (size_t i = 0; i < gch.size(); ++i) {
         IDG_CUDA(cudaStreamWaitEvent(B.s_compute, h2d_done[i], 0));
-        const int64_t s0 = c_begin[i], n = c_begin[i + 1] - s0;
+        const int64_t s0 = gch[i].s0, n = gch[i].s1 - s0;
         if (int rc = idg_grid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,
                                            (const float *)B.k, B.vis_in, (const float *)B.taper, B.aterms,
                                            static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
@@ -260,8 +309,8 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
 
     // degridding phase (rows the plan does not name come back as zeros)
     IDG_CUDA(cudaMemsetAsync(B.vis_out, 0, b_vis, B.s_compute));
-    for (size_t i = 0; i < nchunks; ++i) {
-        const int64_t s0 = c_begin[i], n = c_begin[i + 1] - s0;
+    for (size_t i = 0; i < dch.size(); ++i) {
+        const int64_t s0 = dch[i].s0, n = dch[i].s1 - s0;
         if (int rc = idg_degrid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,
                                              (const float *)B.k, B.vis_out, (const float *)B.taper, B.aterms,
                                              static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
@@ -270,7 +319,7 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         launches += 3;
         IDG_CUDA(cudaEventRecord(deg_done[i], B.s_compute));
         IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, deg_done[i], 0));
-        const size_t off = (size_t)c_rows0[i] * C * 32, bytes = (size_t)(c_rows1[i] - c_rows0[i]) * C * 32;
+        const size_t off = (size_t)dch[i].r0 * C * 32, bytes = (size_t)(dch[i].r1 - dch[i].r0) * C * 32;
         IDG_CUDA(cudaEventRecord(d2h_b[i], B.s_d2h));
         IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(visibilities_out) + off, static_cast<char *>(B.vis_out) + off,
                                  bytes, cudaMemcpyDeviceToHost, B.s_d2h));
@@ -308,7 +357,7 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         float hv = 0;
         IDG_CUDA(cudaEventElapsedTime(&hv, h2d_v0, h2d_v1));
         double dv = 0;
-        for (size_t i = 0; i < nchunks; ++i) {
+        for (size_t i = 0; i < dch.size(); ++i) {
             float x = 0;
             IDG_CUDA(cudaEventElapsedTime(&x, d2h_b[i], d2h_e[i]));
             dv += x;
@@ -317,6 +366,8 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         timing->d2h_vis_ms = dv;
         timing->h2d_vis_bytes = h2d_vis;
         timing->d2h_vis_bytes = d2h_vis;
+        timing->grid_chunks = (int64_t)gch.size();
+        timing->degrid_chunks = (int64_t)dch.size();
     }
     return IDG_OK;
 }

@@ -101,7 +101,12 @@ class IdgCycleTiming(ctypes.Structure):
         ("d2h_vis_ms", ctypes.c_double),
         ("h2d_vis_bytes", ctypes.c_int64),
         ("d2h_vis_bytes", ctypes.c_int64),
+        ("grid_chunks", ctypes.c_int64),
+        ("degrid_chunks", ctypes.c_int64),
     ]
+
+
+CHUNKS_AUTO = -1  # IDG_CHUNKS_AUTO: idg_imaging_cycle sizes its chunks for the copy pipeline
 
 
 class IdgServerConfig(ctypes.Structure):

@@ -422,7 +422,42 @@ def test_plan_steps_and_graph_cycle_match_direct_calls(oracle_mod, idg):
         plan.close()
 
 
-@pytest.mark.parametrize("chunk", [0, 5])
+def test_host_buffer_cycle_auto_chunks(idg):
+    """IDG_CHUNKS_AUTO on 8192 config-2 subgrids: chunks growing through the
+    gridding phase and shrinking through the degridding phase (several of
+    each), uvw rows travelling with their chunk; same grid and visibilities as
+    the device-resident steps."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    spec = D.config2()
+    obs = D.truncate_observation(D.make_observation(spec), 8192)
+    spec = obs.spec
+    S, G, N = spec.subgrid_size, spec.grid_size, spec.n_subgrids
+    gs = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    vis_d = D.visibilities(spec, device="cuda", seed=41)
+    d = {k: dev(v) for k, v in dict(md=obs.metadata, uvw=obs.uvw, k=obs.wavenumbers, taper=obs.taper,
+                                    at=obs.aterms).items()}
+    sub = torch.empty((N, 4, S, S), dtype=torch.complex64, device="cuda")
+    g_ref = torch.zeros((1, 4, G, G), dtype=torch.complex64, device="cuda")
+    ops.grid_visibilities(gs, d["md"], d["uvw"], d["k"], vis_d, d["taper"], d["at"], sub, g_ref)
+    v_ref = torch.zeros_like(vis_d)
+    ops.degrid_visibilities(gs, d["md"], d["uvw"], d["k"], v_ref, d["taper"], d["at"], sub, g_ref)
+    torch.cuda.synchronize()
+    vis_h = vis_d.cpu().numpy()
+    out_h = np.zeros_like(vis_h)
+    grid_h = np.zeros((1, 4, G, G), np.complex64)
+    t = ops.imaging_cycle(gs, obs.metadata, obs.uvw, obs.wavenumbers, vis_h, obs.taper,
+                          np.ascontiguousarray(obs.aterms), out_h, grid_out=grid_h, chunk_subgrids=L.CHUNKS_AUTO)
+    print(f"[cycle] auto chunks: {t['grid_chunks']} gridding, {t['degrid_chunks']} degridding")
+    assert t["grid_chunks"] > 1 and t["degrid_chunks"] > 1
+    assert t["h2d_bytes"] >= vis_h.nbytes + obs.uvw.nbytes
+    check_rel("host cycle auto chunks grid", grid_h, g_ref.cpu().numpy(), TOL)
+    check_rel("host cycle auto chunks vis", out_h, v_ref.cpu().numpy(), TOL)
+    ops.release_buffers()
+
+
+@pytest.mark.parametrize("chunk", [0, 5, -1])
 @pytest.mark.parametrize("locked", [False, True])
 def test_host_buffer_cycle_matches_device_steps(idg, chunk, locked):
     """idg_imaging_cycle on host buffers (pageable numpy arrays, or page-locked
