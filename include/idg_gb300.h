@@ -437,11 +437,12 @@ typedef struct idg_cycle_timing {
  * chunks on their own streams so that transfers overlap the kernels (the
  * plan's rows must then be in chunk order; otherwise the cycle runs as one
  * chunk).  chunk_subgrids > 0: chunks of that many subgrids; IDG_CHUNKS_AUTO:
- * eight chunks per phase whose sizes double from chunk to chunk while
+ * ten chunks per phase whose sizes grow by 1.6x from chunk to chunk while
  * gridding (the first copy in is small, so the kernels start early, and each
- * later copy finishes while the previous chunk is gridded) and halve while
- * degridding (the last copy out is small), at least 1024 subgrids each;
- * 0: one chunk.  uvw rows travel with their chunk.  Device buffers are kept between calls of
+ * later copy finishes while the previous chunk is gridded, for copy rates of
+ * 1.6x the rate the kernels consume) and shrink by 1.6x while degridding (the
+ * last copy out is small), at least 1024 subgrids each; 0: one chunk.  uvw
+ * rows travel with their chunk.  Device buffers are kept between calls of
  * the same sizes and freed by idg_release_buffers().  Pinned host buffers
  * give full copy bandwidth.  The cycle clears the device check word (see
  * idg_device_status) before its first kernel and returns IDG_ERR_DEVICE_CHECK

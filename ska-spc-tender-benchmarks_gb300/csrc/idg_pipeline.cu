@@ -6,6 +6,7 @@
 // The taper moves from the gridder epilogue / degridder prologue into the
 // FFT's pre/post multiplication, where it costs nothing extra.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -54,18 +55,25 @@ struct Chunk {
 };
 
 // Subgrid boundaries 0 = b0 < b1 < ... = n.  chunk > 0: equal chunks of that
-// many subgrids; IDG_CHUNKS_AUTO: eight chunks whose sizes double from one to
-// the next (`growing`) or halve (otherwise), chunks under kMinChunk subgrids
-// merged into their neighbour; anything else: one chunk.
+// many subgrids; IDG_CHUNKS_AUTO: kAutoChunks chunks whose sizes grow by
+// kAutoRatio from one to the next (`growing`) or shrink by it (otherwise),
+// chunks under kMinChunk subgrids merged into their neighbour; anything else:
+// one chunk.  A growing chunk's copy keeps ahead of the previous chunk's
+// kernels while the copy rate is at least kAutoRatio times the rate the
+// kernels consume visibilities (about 61 GB/s for the config-2 gridder:
+// copies at 98 GB/s or more suffice).
 constexpr int64_t kMinChunk = 1024;
+constexpr int kAutoChunks = 10;
+constexpr double kAutoRatio = 1.6;
 std::vector<int64_t> chunk_bounds(int64_t n, int64_t chunk, bool growing) {
     std::vector<int64_t> b{0};
     if (chunk == IDG_CHUNKS_AUTO) {
-        const int k = 8;
-        const double total = (double)((1 << k) - 1);
+        const int k = kAutoChunks;
+        double total = 0;
+        for (int i = 0; i < k; ++i) total += std::pow(kAutoRatio, i);
         double acc = 0;
         for (int i = 0; i < k; ++i) {
-            acc += (double)(1 << (growing ? i : k - 1 - i));
+            acc += std::pow(kAutoRatio, growing ? i : k - 1 - i);
             const int64_t e = i == k - 1 ? n : (int64_t)(n * acc / total + 0.5);
             if (e - b.back() >= kMinChunk) b.push_back(e);
         }
