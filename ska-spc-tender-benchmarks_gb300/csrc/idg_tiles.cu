@@ -12,7 +12,7 @@
 //    tile's list is ascending).  Each list is cut into chunks of at most
 //    kChunk subgrids.
 //  * Pass 1, one CTA per chunk: the chunk's plan entries are staged in shared
-//    memory; every thread owns four cells of one column of the tile (all four
+//    memory; every thread owns two cells of one column of the tile (all four
 //    correlations) and adds the chunk's subgrids into registers, in list
 //    order.  A tile with one chunk is then added into the
 //    grid with plain loads and stores -- no other CTA touches it; a tile with
@@ -35,7 +35,7 @@ namespace idg {
 namespace {
 
 constexpr int kTile = 32;       // tile edge in cells (one warp lane per column)
-constexpr int kWarps = 8;       // rows of a tile shared out over 8 warps, 4 rows each
+constexpr int kWarps = 16;      // rows of a tile shared out over 16 warps, 2 rows each
 constexpr int kRowsPerThread = kTile / kWarps;
 constexpr int kChunk = 128;     // subgrids per pass-1 work item
 
