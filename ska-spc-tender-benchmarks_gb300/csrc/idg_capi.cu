@@ -33,10 +33,11 @@ std::vector<DeviceWords> g_words;
 // Launch shapes of the batched kernels per (device, subgrid size), set by the
 // autotuner or by idg_set_batched_shapes().  Until then, the shapes measured
 // fastest on GB300: the mirror-quad gridder with 64 threads x 4 quads (shape
-// 22) where 64 threads cover whole quad columns (S/2 divides 64), else the
-// Gauss pixel-pair shapes that make whole passes for S = 24 (11) and 48 (12);
-// the mirror-quad degridder with kappa from shared memory, in column form
-// (shape 32) or row by row (shape 31).
+// 22; 24 with 512-visibility tiles for S = 32) where 64 threads cover whole
+// quad columns (S/2 divides 64), else the Gauss pixel-pair shapes that make
+// whole passes for S = 24 (11) and 48 (12); the mirror-quad degridder with
+// kappa from shared memory, in column form (shape 32; 34 with its runs of
+// four quads for S = 32) or row by row (shape 31).
 std::mutex g_shape_mutex;
 std::map<std::pair<int, int>, std::pair<int, int>> g_shapes;
 
@@ -49,8 +50,8 @@ int current_device() {
 // Degridder: the column form (32) where each lane's quads run down a column
 // for at least four steps (S a multiple of 8, S >= 32), else the row form (31).
 std::pair<int, int> default_shapes(int S) {
-    const int g = (S >= 2 && 64 % (S / 2) == 0) ? 22 : S == 24 ? 11 : S == 48 ? 12 : 13;
-    const int d = (S >= 32 && S % 8 == 0) ? 32 : 31;
+    const int g = S == 32 ? 24 : (S >= 2 && 64 % (S / 2) == 0) ? 22 : S == 24 ? 11 : S == 48 ? 12 : 13;
+    const int d = S == 32 ? 34 : (S >= 32 && S % 8 == 0) ? 32 : 31;
     return {g < gridder_fast_shapes() ? g : 0, d < degridder_fast_shapes() ? d : 0};
 }
 

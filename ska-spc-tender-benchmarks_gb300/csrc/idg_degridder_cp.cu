@@ -397,6 +397,53 @@ __host__ __device__ inline QuadLayout quad_layout(int S, int C, int batch) {
     return L;
 }
 
+// Stages quad (gx, gy) of subgrid s: its pixels 0 = (gx, gy),
+// 1 = (S-1-gx, S-1-gy), 2 = (S-1-gx, gy), 3 = (gx, S-1-gy) with taper and
+// A-terms applied, as the operands the quad MACs read.  With e the sums and
+// differences of the pixels that Z = P00 conj(X) + P11 X + P10 conj(Y) + P01 Y
+// takes (Zr = Xr e0 + Xi e1 + Yr e2 + Yi e3, Zi likewise with e4..e7), and
+// Xr = m1 - m2, Yr = m1 + m2, Xi = m3 + m4, Yi = m3 - m4 for the products
+// m1 = Pc Qc, m2 = Ps Qs, m3 = Pc Qs, m4 = Ps Qc, the operands are
+// f = (e0 + e2, e2 - e0, e1 + e3, e1 - e3, e4 + e6, e6 - e4, e5 + e7, e5 - e7):
+// Zr = m1 f0 + m2 f1 + m3 f2 + m4 f3, Zi = m1 f4 + m2 f5 + m3 f6 + m4 f7.
+// Correlation k's eight operands go to d[kstride * k + r], r < 4, each float4
+// two operands, each duplicated into both packed halves.
+__device__ __forceinline__ void stage_quad(const KernelArgs &a, int s, int gx, int gy, const float4 *a1,
+                                           const float4 *a2, bool taper, bool refcpu, float4 *d, int kstride) {
+    const int S = a.S, S2 = S * S;
+    const int qx[4] = {gx, S - 1 - gx, S - 1 - gx, gx};
+    const int qy[4] = {gy, S - 1 - gy, gy, S - 1 - gy};
+    cf v[4][4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int q = qy[e] * S + qx[e];
+        const float sph = taper ? a.taper[q] : 1.f;
+#pragma unroll
+        for (int pol = 0; pol < 4; ++pol) {
+            const float2 x = a.subgrids[((size_t)s * 4 + pol) * S2 + q];
+            v[e][pol] = {sph * x.x, sph * x.y};
+        }
+        cf j1[4], j2[4];
+        load_jones(a1 + 2 * q, j1);
+        load_jones(a2 + 2 * q, j2);
+        if (refcpu)
+            aterm_gridder(v[e], j1, j2);
+        else
+            aterm_adjoint(v[e], j1, j2);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const cf p00 = v[0][k], p11 = v[1][k], p10 = v[2][k], p01 = v[3][k];
+        const float e[8] = {p00.re + p11.re, p00.im - p11.im, p10.re + p01.re, p10.im - p01.im,
+                            p00.im + p11.im, p11.re - p00.re, p10.im + p01.im, p01.re - p10.re};
+        const float f[8] = {e[0] + e[2], e[2] - e[0], e[1] + e[3], e[1] - e[3],
+                            e[4] + e[6], e[6] - e[4], e[5] + e[7], e[5] - e[7]};
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            d[kstride * k + r] = make_float4(f[2 * r], f[2 * r], f[2 * r + 1], f[2 * r + 1]);
+    }
+}
+
 // KP: the channel pairs' kappa, either f2 registers (f2[NPAIR]) or a pointer
 // to the group's first channel in shared memory (read per channel pair).
 __device__ __forceinline__ f2 kappa_pair(const f2 (&kp)[4], int j) { return kp[j]; }
@@ -428,15 +475,13 @@ __device__ __forceinline__ void quad_macs(f2 (&acc)[NPAIR][4][2], const KP &kp, 
         sincos_pair(ap, Pc, Ps);
         sincos_pair(aq, Qc, Qs);
         sincos_pair(ar, Rc, Rs);
-        const f2 nPs = neg2(Ps), nRs = neg2(Rs);
-        const f2 m1 = fmul2(Pc, Qc), m3 = fmul2(Pc, Qs);
-        const f2 Xr = ffma2(nPs, Qs, m1), Yr = ffma2(Ps, Qs, m1);
-        const f2 Xi = ffma2(Ps, Qc, m3), Yi = ffma2(nPs, Qc, m3);
+        const f2 nRs = neg2(Rs);
+        const f2 m1 = fmul2(Pc, Qc), m2 = fmul2(Ps, Qs), m3 = fmul2(Pc, Qs), m4 = fmul2(Ps, Qc);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const f2 *p = o + 8 * k;
-            const f2 Zr = ffma2(Yi, p[3], ffma2(Yr, p[2], ffma2(Xi, p[1], fmul2(Xr, p[0]))));
-            const f2 Zi = ffma2(Yi, p[7], ffma2(Yr, p[6], ffma2(Xi, p[5], fmul2(Xr, p[4]))));
+            const f2 Zr = ffma2(m4, p[3], ffma2(m3, p[2], ffma2(m2, p[1], fmul2(m1, p[0]))));
+            const f2 Zi = ffma2(m4, p[7], ffma2(m3, p[6], ffma2(m2, p[5], fmul2(m1, p[4]))));
             // V += conj(R) Z
             acc[j][k][0] = ffma2(Rs, Zi, ffma2(Rc, Zr, acc[j][k][0]));
             acc[j][k][1] = ffma2(nRs, Zr, ffma2(Rc, Zi, acc[j][k][1]));
@@ -487,15 +532,13 @@ __device__ __forceinline__ void quad_macs_col(f2 (&acc)[NPAIR][4][2], const f2 (
         f2 Qc, Qs, Rc, Rs;
         sincos_pair(aq, Qc, Qs);
         sincos_pair(ar, Rc, Rs);
-        const f2 nPs = neg2(Ps[j]), nRs = neg2(Rs);
-        const f2 m1 = fmul2(Pc[j], Qc), m3 = fmul2(Pc[j], Qs);
-        const f2 Xr = ffma2(nPs, Qs, m1), Yr = ffma2(Ps[j], Qs, m1);
-        const f2 Xi = ffma2(Ps[j], Qc, m3), Yi = ffma2(nPs, Qc, m3);
+        const f2 nRs = neg2(Rs);
+        const f2 m1 = fmul2(Pc[j], Qc), m2 = fmul2(Ps[j], Qs), m3 = fmul2(Pc[j], Qs), m4 = fmul2(Ps[j], Qc);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const f2 *p = o + 8 * k;
-            const f2 Zr = ffma2(Yi, p[3], ffma2(Yr, p[2], ffma2(Xi, p[1], fmul2(Xr, p[0]))));
-            const f2 Zi = ffma2(Yi, p[7], ffma2(Yr, p[6], ffma2(Xi, p[5], fmul2(Xr, p[4]))));
+            const f2 Zr = ffma2(m4, p[3], ffma2(m3, p[2], ffma2(m2, p[1], fmul2(m1, p[0]))));
+            const f2 Zi = ffma2(m4, p[7], ffma2(m3, p[6], ffma2(m2, p[5], fmul2(m1, p[4]))));
             acc[j][k][0] = ffma2(Rs, Zi, ffma2(Rc, Zr, acc[j][k][0]));
             acc[j][k][1] = ffma2(nRs, Zr, ffma2(Rc, Zi, acc[j][k][1]));
         }
@@ -514,7 +557,7 @@ __device__ __forceinline__ void quad_macs_col_pf(f2 (&acc)[NPAIR][4][2], const f
     const f2 TY = pack2(ty, ty), TN = pack2(tn, tn);
     const float qy = qv * g.y, qn = qw * g.z;
     const f2 QY = pack2(qy, qy), QN = pack2(qn, qn);
-    f2 Xr[NPAIR], Xi[NPAIR], Yr[NPAIR], Yi[NPAIR], Rc[NPAIR], Rs[NPAIR];
+    f2 m1[NPAIR], m2[NPAIR], m3[NPAIR], m4[NPAIR], Rc[NPAIR], Rs[NPAIR];
 #pragma unroll
     for (int j = 0; j < NPAIR; ++j) {
         const f2 kj = kappa_pair(kp, j);
@@ -526,12 +569,10 @@ __device__ __forceinline__ void quad_macs_col_pf(f2 (&acc)[NPAIR][4][2], const f
         f2 Qc, Qs;
         sincos_pair(aq, Qc, Qs);
         sincos_pair(ar, Rc[j], Rs[j]);
-        const f2 nPs = neg2(Ps[j]);
-        const f2 m1 = fmul2(Pc[j], Qc), m3 = fmul2(Pc[j], Qs);
-        Xr[j] = ffma2(nPs, Qs, m1);
-        Yr[j] = ffma2(Ps[j], Qs, m1);
-        Xi[j] = ffma2(Ps[j], Qc, m3);
-        Yi[j] = ffma2(nPs, Qc, m3);
+        m1[j] = fmul2(Pc[j], Qc);
+        m2[j] = fmul2(Ps[j], Qs);
+        m3[j] = fmul2(Pc[j], Qs);
+        m4[j] = fmul2(Ps[j], Qc);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -540,8 +581,8 @@ __device__ __forceinline__ void quad_macs_col_pf(f2 (&acc)[NPAIR][4][2], const f
         for (int q = 0; q < 4; ++q) lds2(ops_addr + 64 * k + 16 * q, p[2 * q], p[2 * q + 1]);
 #pragma unroll
         for (int j = 0; j < NPAIR; ++j) {
-            const f2 Zr = ffma2(Yi[j], p[3], ffma2(Yr[j], p[2], ffma2(Xi[j], p[1], fmul2(Xr[j], p[0]))));
-            const f2 Zi = ffma2(Yi[j], p[7], ffma2(Yr[j], p[6], ffma2(Xi[j], p[5], fmul2(Xr[j], p[4]))));
+            const f2 Zr = ffma2(m4[j], p[3], ffma2(m3[j], p[2], ffma2(m2[j], p[1], fmul2(m1[j], p[0]))));
+            const f2 Zi = ffma2(m4[j], p[7], ffma2(m3[j], p[6], ffma2(m2[j], p[5], fmul2(m1[j], p[4]))));
             acc[j][k][0] = ffma2(Rs[j], Zi, ffma2(Rc[j], Zr, acc[j][k][0]));
             acc[j][k][1] = ffma2(neg2(Rs[j]), Zr, ffma2(Rc[j], Zi, acc[j][k][1]));
         }
@@ -653,37 +694,7 @@ __device__ __forceinline__ void degridder_quad_body(const KernelArgs &a) {
             for (int i = tid; i < nq; i += kT) {
                 const int g = qb + i;
                 const int gy = COL ? g % Sh : g / Sh, gx = COL ? g / Sh : g % Sh;
-                // 0 = (gx, gy), 1 = (S-1-gx, S-1-gy), 2 = (S-1-gx, gy), 3 = (gx, S-1-gy)
-                const int qx[4] = {gx, S - 1 - gx, S - 1 - gx, gx};
-                const int qy[4] = {gy, S - 1 - gy, gy, S - 1 - gy};
-                cf v[4][4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int q = qy[e] * S + qx[e];
-                    const float sph = taper ? a.taper[q] : 1.f;
-#pragma unroll
-                    for (int pol = 0; pol < 4; ++pol) {
-                        const float2 x = a.subgrids[((size_t)s * 4 + pol) * S2 + q];
-                        v[e][pol] = {sph * x.x, sph * x.y};
-                    }
-                    cf j1[4], j2[4];
-                    load_jones(a1 + 2 * q, j1);
-                    load_jones(a2 + 2 * q, j2);
-                    if (refcpu)
-                        aterm_gridder(v[e], j1, j2);
-                    else
-                        aterm_adjoint(v[e], j1, j2);
-                }
-                float4 *d = ops + (kQuadStride / 16) * i;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const cf p00 = v[0][k], p11 = v[1][k], p10 = v[2][k], p01 = v[3][k];
-                    const float e8[8] = {p00.re + p11.re, p00.im - p11.im, p10.re + p01.re, p10.im - p01.im,
-                                         p00.im + p11.im, p11.re - p00.re, p10.im + p01.im, p01.re - p10.re};
-#pragma unroll
-                    for (int r = 0; r < 4; ++r)
-                        d[4 * k + r] = make_float4(e8[2 * r], e8[2 * r], e8[2 * r + 1], e8[2 * r + 1]);
-                }
+                stage_quad(a, s, gx, gy, a1, a2, taper, refcpu, ops + (kQuadStride / 16) * i, 4);
                 const float3 gg = pixel_geometry(gy * S + gx, S, a.image_size);
                 geo[i] = make_float4(gg.x, gg.y, gg.z, 0.f);
             }
@@ -773,6 +784,287 @@ __global__ void __maxnreg__(MAXR) degridder_quad_kernel_r(KernelArgs a) {
     degridder_quad_body<NT, QB, CB, UNR, KSM, COL, RUN, PF>(a);
 }
 
+// ---------------------------------------------------------------------------
+// Swap-symmetric octets (degridder_oct_kernel).  Quad (a, b) and its transpose
+// (b, a) hold pixels with the same n (l and m swap), so one R = e^{i g n}
+// serves eight pixels.  With quad 1 = (a, b) and quad 2 = (b, a), a < b,
+//   V += conj(R) (Z1 + Z2),
+// Z1 from P = P(ha), Q = Q(hb) and quad 1's operands, Z2 likewise from
+// P(hb), Q(ha) and quad 2's: 8 FMA per correlation for each Z, and the
+// rotation by conj(R) (4 FMA) is shared.  A correlation costs 20 FMA per
+// eight pixels instead of 24; per pixel and channel 11.6 FMA (13.5 for
+// quads) and 1.25 sincos (1.125).  The diagonal quads (a, a) are their own
+// transposes and stay quads.
+// The factors of all channel pairs are formed first (88 registers), then the
+// operands are read one correlation at a time (32 registers): a whole octet's
+// operands (128 registers) would not fit beside the accumulators.  Forming
+// the factors two channel pairs at a time (operands read twice) needs as many
+// registers, and at 12 warps per SM both forms spill heavily.
+// ---------------------------------------------------------------------------
+// 512 B of operands per octet padded to 528 B: the four lanes of a group read
+// octets 132 words = 4 banks apart.
+constexpr uint32_t kOctStride = 528;
+
+struct OctLayout {
+    size_t ops, diag, geo, dgeo, coef, kappa, total;
+    int ob;  // octets per batch
+};
+
+__host__ __device__ inline OctLayout oct_layout(int S, int C, int ob_max) {
+    const int Sh = S / 2, no = Sh * (Sh - 1) / 2;
+    OctLayout L;
+    L.ob = no < ob_max ? no : ob_max;
+    size_t off = 64;
+    L.ops = off;   off += (size_t)L.ob * kOctStride;      // octet operands, per correlation quad 1 then quad 2
+    L.diag = off;  off += (size_t)Sh * kQuadStride;       // the Sh diagonal quads (last batch)
+    L.geo = off;   off += (size_t)L.ob * 16;              // (ha, hb, n, 0) of pixel (a, b)
+    L.dgeo = off;  off += (size_t)Sh * 16;
+    L.coef = off;  off += (size_t)kTimeTile * 32;         // (a, b, g, qu) (qv, qw, -, -) per timestep
+    L.kappa = off; off += (size_t)(C + kMaxCB) * 4;       // kappa per channel, zero padded
+    L.total = (off + 15) & ~size_t(15);
+    return L;
+}
+
+// Octet index u (row-major over a < b) -> (a, b).
+__device__ __forceinline__ void octet_coords(int u, int Sh, int &a, int &b) {
+    int r = 0;
+    while (u >= Sh - 1 - r) {
+        u -= Sh - 1 - r;
+        ++r;
+    }
+    a = r;
+    b = r + 1 + u;
+}
+
+// g = (ha, hb, n, 0); c0 = (A, B, G, qu), c1 = (qv, qw, -, -).
+template <int NPAIR, bool FAST>
+__device__ __forceinline__ void oct_macs(f2 (&acc)[NPAIR][4][2], const float *kp, float4 g, float4 c0, float4 c1,
+                                         uint32_t ops_addr) {
+    const float A = c0.x, B = c0.y, Gc = c0.z, qu = c0.w, qv = c1.x, qw = c1.y;
+    const float tp1 = reduce_2pi_s(A * g.x), tq1 = reduce_2pi_s(B * g.y);
+    const float tp2 = reduce_2pi_s(A * g.y), tq2 = reduce_2pi_s(B * g.x);
+    const float tn = reduce_2pi_s(Gc * g.z);
+    const float sp1 = qu * g.x, sq1 = qv * g.y, sp2 = qu * g.y, sq2 = qv * g.x, sn = qw * g.z;
+    const f2 TP1 = pack2(tp1, tp1), TQ1 = pack2(tq1, tq1), TP2 = pack2(tp2, tp2), TQ2 = pack2(tq2, tq2),
+             TN = pack2(tn, tn);
+    const f2 SP1 = pack2(sp1, sp1), SQ1 = pack2(sq1, sq1), SP2 = pack2(sp2, sp2), SQ2 = pack2(sq2, sq2),
+             SN = pack2(sn, sn);
+    f2 a1[NPAIR], a2[NPAIR], a3[NPAIR], a4[NPAIR];  // quad 1's m1..m4
+    f2 b1[NPAIR], b2[NPAIR], b3[NPAIR], b4[NPAIR];  // quad 2's
+    f2 Rc[NPAIR], Rs[NPAIR], nRs[NPAIR];
+#pragma unroll
+    for (int j = 0; j < NPAIR; ++j) {
+        const f2 kj = kappa_pair(kp, j);
+        f2 ap1 = ffma2(kj, SP1, TP1), aq1 = ffma2(kj, SQ1, TQ1);
+        f2 ap2 = ffma2(kj, SP2, TP2), aq2 = ffma2(kj, SQ2, TQ2), ar = ffma2(kj, SN, TN);
+        if (!FAST) {
+            ap1 = reduce_2pi(ap1);
+            aq1 = reduce_2pi(aq1);
+            ap2 = reduce_2pi(ap2);
+            aq2 = reduce_2pi(aq2);
+            ar = reduce_2pi(ar);
+        }
+        f2 Pc, Ps, Qc, Qs;
+        sincos_pair(ap1, Pc, Ps);
+        sincos_pair(aq1, Qc, Qs);
+        a1[j] = fmul2(Pc, Qc);
+        a2[j] = fmul2(Ps, Qs);
+        a3[j] = fmul2(Pc, Qs);
+        a4[j] = fmul2(Ps, Qc);
+        sincos_pair(ap2, Pc, Ps);
+        sincos_pair(aq2, Qc, Qs);
+        b1[j] = fmul2(Pc, Qc);
+        b2[j] = fmul2(Ps, Qs);
+        b3[j] = fmul2(Pc, Qs);
+        b4[j] = fmul2(Ps, Qc);
+        sincos_pair(ar, Rc[j], Rs[j]);
+        nRs[j] = neg2(Rs[j]);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        f2 p[16];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) lds2(ops_addr + 128 * k + 16 * q, p[2 * q], p[2 * q + 1]);
+#pragma unroll
+        for (int j = 0; j < NPAIR; ++j) {
+            f2 Zr = fmul2(a1[j], p[0]);
+            Zr = ffma2(a2[j], p[1], Zr);
+            Zr = ffma2(a3[j], p[2], Zr);
+            Zr = ffma2(a4[j], p[3], Zr);
+            Zr = ffma2(b1[j], p[8], Zr);
+            Zr = ffma2(b2[j], p[9], Zr);
+            Zr = ffma2(b3[j], p[10], Zr);
+            Zr = ffma2(b4[j], p[11], Zr);
+            f2 Zi = fmul2(a1[j], p[4]);
+            Zi = ffma2(a2[j], p[5], Zi);
+            Zi = ffma2(a3[j], p[6], Zi);
+            Zi = ffma2(a4[j], p[7], Zi);
+            Zi = ffma2(b1[j], p[12], Zi);
+            Zi = ffma2(b2[j], p[13], Zi);
+            Zi = ffma2(b3[j], p[14], Zi);
+            Zi = ffma2(b4[j], p[15], Zi);
+            acc[j][k][0] = ffma2(Rs[j], Zi, ffma2(Rc[j], Zr, acc[j][k][0]));
+            acc[j][k][1] = ffma2(nRs[j], Zr, ffma2(Rc[j], Zi, acc[j][k][1]));
+        }
+    }
+}
+
+// Work split as in the quad kernel (a group is one timestep x CB channels,
+// four lanes split the staged units).  A subgrid's Sh (Sh - 1) / 2 octets are
+// staged in batches of at most OB; the last batch also holds the Sh diagonal
+// quads.  S = 32: one batch of 120 octets and 16 quads, 30 + 4 per lane.
+template <int NT, int OB, int CB>
+__device__ __forceinline__ void degridder_oct_body(const KernelArgs &a) {
+    constexpr int kT = NT, kCB = CB, kNP = CB / 2;
+    static_assert(CB == 4 || CB == 8, "channel groups of 4 or 8");
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int S = a.S, S2 = S * S, Sh = S / 2, no = Sh * (Sh - 1) / 2;
+    const OctLayout L = oct_layout(S, a.C, OB);
+    const int nbatch = no > 0 ? (no + L.ob - 1) / L.ob : 1;
+    Head *head = reinterpret_cast<Head *>(smem);
+    float4 *ops = reinterpret_cast<float4 *>(smem + L.ops);
+    float4 *dops = reinterpret_cast<float4 *>(smem + L.diag);
+    float4 *geo = reinterpret_cast<float4 *>(smem + L.geo);
+    float4 *dgeo = reinterpret_cast<float4 *>(smem + L.dgeo);
+    float4 *coef = reinterpret_cast<float4 *>(smem + L.coef);
+    float *kap = reinterpret_cast<float *>(smem + L.kappa);
+    const uint32_t ops_addr = smem_addr(ops), dops_addr = smem_addr(dops);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gw = lane / kLanes, part = lane % kLanes;
+    const bool refcpu = (a.flags & IDG_FLAG_DEGRID_ATERM_REFCPU) != 0;
+    const bool taper = (a.flags & IDG_FLAG_NO_TAPER) == 0;
+    const double d2pi = (double)a.image_size / (double)S / kTwoPi;
+    const float hmax = 0.5f * (float)(S - 1);
+    const float nmax = pixel_geometry(0, S, a.image_size).z;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            head->next = atomicAdd(a.work_counter, 1);
+            head->kmax_bits = 0;
+            head->qmax_bits = 0;
+        }
+        __syncthreads();
+        const int idx = head->next;
+        if (idx >= a.nr_subgrids) break;
+        const int s = a.work_list ? a.work_list[idx] : idx;
+        const SubgridInfo si = load_subgrid(a, s);
+        if (!si.ok) {
+            if (tid == 0) flag_status(a.status, kStatusBadPlan);
+            continue;
+        }
+        const int nc = si.c1 - si.c0;
+        const int ncb = (nc + kCB - 1) / kCB;
+        const int cref = si.c0 + (nc > 0 ? (nc - 1) / 2 : 0);
+        const double kref = nc > 0 ? (double)a.wavenumbers[cref] : 0.0;
+        float kmax = 0.f;
+        for (int c = tid; c < ncb * kCB; c += kT) {
+            float kv = 0.f;
+            if (c < nc) kv = (float)((double)a.wavenumbers[si.c0 + c] - kref);
+            kap[c] = kv;
+            kmax = fmaxf(kmax, fabsf(kv));
+        }
+        if (kmax > 0.f) atomicMax(&head->kmax_bits, __float_as_int(kmax));
+        const size_t jones_stride = (size_t)S2 * 2;
+        const float4 *a1 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st1) * jones_stride;
+        const float4 *a2 = a.aterms + ((size_t)si.aterm * a.nr_stations + si.st2) * jones_stride;
+
+        for (int b = 0; b < nbatch; ++b) {
+            const int o0 = b * L.ob;
+            const int nob = no - o0 < L.ob ? no - o0 : L.ob;
+            const int nd = b == nbatch - 1 ? Sh : 0;
+            __syncthreads(); // previous batch consumed
+            for (int i = tid; i < nob + nd; i += kT) {
+                if (i < nob) {
+                    int oa, ob;
+                    octet_coords(o0 + i, Sh, oa, ob);
+                    float4 *d = ops + (kOctStride / 16) * i;
+                    stage_quad(a, s, oa, ob, a1, a2, taper, refcpu, d, 8);
+                    stage_quad(a, s, ob, oa, a1, a2, taper, refcpu, d + 4, 8);
+                    const float3 gg = pixel_geometry(ob * S + oa, S, a.image_size);
+                    geo[i] = make_float4(gg.x, gg.y, gg.z, 0.f);
+                } else {
+                    const int dq = i - nob;
+                    stage_quad(a, s, dq, dq, a1, a2, taper, refcpu, dops + (kQuadStride / 16) * dq, 4);
+                    const float3 gg = pixel_geometry(dq * S + dq, S, a.image_size);
+                    dgeo[dq] = make_float4(gg.x, gg.y, gg.z, 0.f);
+                }
+            }
+
+            for (int t0 = 0; t0 < si.T; t0 += kTimeTile) {
+                const int tt = min(kTimeTile, si.T - t0);
+                const bool fast = tile_coefficients<kT, false>(a, si, head, coef, t0, tt, kref, d2pi, hmax, nmax);
+                const int ngroups = tt * ncb;
+                for (int gbase = warp * kGroupsPerWarp; gbase < ngroups; gbase += (kT / 32) * kGroupsPerWarp) {
+                    const int grp = gbase + gw;
+                    const bool active = grp < ngroups;
+                    const int gg = active ? grp : 0;
+                    const int t = gg / ncb, cfirst = (gg - t * ncb) * kCB;
+                    const float4 c0 = coef[2 * t], c1 = coef[2 * t + 1];
+                    f2 acc[kNP][4][2];
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j)
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) acc[j][k][0] = acc[j][k][1] = 0ull;
+                    const float *kps = kap + cfirst;
+                    if (fast) {
+                        for (int i = part; i < nob; i += kLanes)
+                            oct_macs<kNP, true>(acc, kps, geo[i], c0, c1, ops_addr + kOctStride * (uint32_t)i);
+                        for (int i = part; i < nd; i += kLanes)
+                            quad_macs<kNP, true>(acc, kps, dgeo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                 dops_addr + kQuadStride * (uint32_t)i);
+                    } else {
+                        for (int i = part; i < nob; i += kLanes)
+                            oct_macs<kNP, false>(acc, kps, geo[i], c0, c1, ops_addr + kOctStride * (uint32_t)i);
+                        for (int i = part; i < nd; i += kLanes)
+                            quad_macs<kNP, false>(acc, kps, dgeo[i], c0.x, c0.y, c0.z, c0.w, c1.x, c1.y,
+                                                  dops_addr + kQuadStride * (uint32_t)i);
+                    }
+                    f2 out[kNP][8];
+#pragma unroll
+                    for (int j = 0; j < kNP; ++j)
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+#pragma unroll
+                            for (int r = 0; r < 2; ++r) {
+                                f2 v = acc[j][k][r];
+                                v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 1));
+                                v = fadd2(v, __shfl_xor_sync(0xffffffffu, v, 2));
+                                out[j][2 * k + r] = v;
+                            }
+                    if (active) write_group<kNP>(a, si, si.row0 + t0 + t, cfirst, nc, part, b > 0, out);
+                }
+            }
+        }
+    }
+}
+
+template <int NT, int OB, int MINB, int CB>
+__global__ void __launch_bounds__(NT, MINB) degridder_oct_kernel(KernelArgs a) {
+    degridder_oct_body<NT, OB, CB>(a);
+}
+
+template <int NT, int OB, int MINB, int CB>
+cudaError_t launch_oct(const KernelArgs &a, cudaStream_t stream) {
+    if (a.S % 2 != 0) return cudaErrorInvalidValue;
+    void (*kern)(KernelArgs) = degridder_oct_kernel<NT, OB, MINB, CB>;
+    const size_t smem = oct_layout(a.S, a.C, OB).total;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (a.share_den > 1) blocks = blocks / a.share_den > 0 ? blocks / a.share_den : 1;
+    if (a.max_ctas > 0 && blocks > a.max_ctas) blocks = a.max_ctas;
+    if (blocks > a.nr_subgrids) blocks = a.nr_subgrids;
+    kern<<<(unsigned)blocks, NT, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
 template <int NT, int QB, int MINB, int CB, int UNR, bool KSM = false, bool COL = false, int RUN = 0, bool PF = false,
           int MAXR = 0>
 cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
@@ -801,7 +1093,7 @@ cudaError_t launch_quad(const KernelArgs &a, cudaStream_t stream) {
 
 } // namespace
 
-int degridder_cp_shapes() { return 24; }
+int degridder_cp_shapes() { return 25; }
 
 // Channel-pair shapes (index within this family):
 //   0: 128 threads, 8-channel groups, 256-pixel batches, 4 CTAs/SM (16 warps)
@@ -828,6 +1120,7 @@ int degridder_cp_shapes() { return 24; }
 //  21: column form, 96 threads x 3 CTAs/SM (9 warps), 128-quad batches
 //  22: shape 21 with the phasors first
 //  23: shape 17 with runs of 8 quads (S = 64)
+//  24: swap-symmetric octets, 128 threads, 8-channel groups, 128-octet batches, 2 CTAs/SM
 cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int shape) {
     switch (shape) {
     case 18: return launch_quad<128, 256, 2, 8, 1, true, true, 0, true>(a, stream);
@@ -836,6 +1129,7 @@ cudaError_t launch_degridder_cp(const KernelArgs &a, cudaStream_t stream, int sh
     case 21: return launch_quad<96, 128, 3, 8, 1, true, true, 0, false, 224>(a, stream);
     case 22: return launch_quad<96, 128, 3, 8, 1, true, true, 0, true, 224>(a, stream);
     case 23: return launch_quad<128, 256, 2, 8, 1, true, true, 8>(a, stream);
+    case 24: return launch_oct<128, 128, 2, 8>(a, stream);
     case 13: return launch_quad<128, 256, 2, 8, 1>(a, stream);
     case 14: return launch_quad<128, 256, 3, 8, 1>(a, stream);
     case 15: return launch_quad<128, 256, 2, 8, 2>(a, stream);

@@ -607,9 +607,11 @@ __global__ void __launch_bounds__(NT, MINB) gridder_fast_kernel(KernelArgs a) {
 // separately over all visibilities they give both pixels in the epilogue, so a
 // quad costs 8 FMA per correlation per visibility (2 per pixel, against 3 for
 // the Gauss form), plus W = V R (4 per correlation, shared by the quad) and
-// X, Y (6).  Per pixel-visibility: 14.25 FMA and 1.5 SFU operations (three
-// sincos per quad), against 14 FMA and 2 SFU operations per pixel above, and
-// 8 accumulators per pixel instead of 12.
+// the four products m1 = Pc Qc, m2 = Ps Qs, m3 = Pc Qs, m4 = Ps Qc (4) that
+// X and Y are made of: the accumulators sum W times each m, and the epilogue
+// forms Wr Xr = sum Wr (m1 - m2) and so on.  Per pixel-visibility: 13.75 FMA
+// and 1.5 SFU operations (three sincos per quad), against 14 FMA and 2 SFU
+// operations per pixel above, and 8 accumulators per pixel instead of 12.
 // Each thread owns GP pairs of quads; the two quads of a pair sit in the two
 // halves of the packed FP32x2 registers.  Per (timestep, quad pair) the
 // factors' offsets tau = A hx, B hy, G n are reduced to [-pi, pi] once; per
@@ -673,11 +675,9 @@ __device__ __forceinline__ void quad_tile(f2 (&acc)[GP][4][8], const f2 *qg, con
                 }
                 sincos_pair<false>(aq, Qc, Qs);
                 sincos_pair<false>(ar, Rc, Rs);
-                // X = P Q, Y = conj(P) Q
-                const f2 nPs = neg2(Ps);
-                const f2 m1 = fmul2(Pc, Qc), m3 = fmul2(Pc, Qs);
-                const f2 Xr = ffma2(nPs, Qs, m1), Yr = ffma2(Ps, Qs, m1);
-                const f2 Xi = ffma2(Ps, Qc, m3), Yi = ffma2(nPs, Qc, m3);
+                // the products X and Y are made of: Xr = m1 - m2, Yr = m1 + m2,
+                // Xi = m3 + m4, Yi = m3 - m4
+                const f2 m1 = fmul2(Pc, Qc), m2 = fmul2(Ps, Qs), m3 = fmul2(Pc, Qs), m4 = fmul2(Ps, Qc);
                 const f2 nRs = neg2(Rs);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
@@ -685,14 +685,14 @@ __device__ __forceinline__ void quad_tile(f2 (&acc)[GP][4][8], const f2 *qg, con
                     const f2 Wr = ffma2(vr[k], Rc, fmul2(vi[k], nRs));
                     const f2 Wi = ffma2(vr[k], Rs, fmul2(vi[k], Rc));
                     f2 *q = acc[j][k];
-                    q[0] = ffma2(Wr, Xr, q[0]);
-                    q[1] = ffma2(Wi, Xi, q[1]);
-                    q[2] = ffma2(Wr, Xi, q[2]);
-                    q[3] = ffma2(Wi, Xr, q[3]);
-                    q[4] = ffma2(Wr, Yr, q[4]);
-                    q[5] = ffma2(Wi, Yi, q[5]);
-                    q[6] = ffma2(Wr, Yi, q[6]);
-                    q[7] = ffma2(Wi, Yr, q[7]);
+                    q[0] = ffma2(Wr, m1, q[0]);
+                    q[1] = ffma2(Wr, m2, q[1]);
+                    q[2] = ffma2(Wi, m1, q[2]);
+                    q[3] = ffma2(Wi, m2, q[3]);
+                    q[4] = ffma2(Wr, m3, q[4]);
+                    q[5] = ffma2(Wr, m4, q[5]);
+                    q[6] = ffma2(Wi, m3, q[6]);
+                    q[7] = ffma2(Wi, m4, q[7]);
                 }
             }
         }
@@ -847,13 +847,17 @@ __global__ void __launch_bounds__(NT, MINB) gridder_quad_kernel(KernelArgs a) {
                     cf px[4][4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        float r[8];
+                        float m[8];
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
                             float lo, hi;
                             unpack2(acc[j][k][i], lo, hi);
-                            r[i] = h ? hi : lo;
+                            m[i] = h ? hi : lo;
                         }
+                        // sums of Wr m1, Wr m2, Wi m1, Wi m2, Wr m3, Wr m4, Wi m3, Wi m4 ->
+                        // Wr Xr, Wi Xi, Wr Xi, Wi Xr, Wr Yr, Wi Yi, Wr Yi, Wi Yr
+                        const float r[8] = {m[0] - m[1], m[6] + m[7], m[4] + m[5], m[2] - m[3],
+                                            m[0] + m[1], m[6] - m[7], m[4] - m[5], m[2] + m[3]};
                         px[0][k] = {r[0] - r[1], r[2] + r[3]};
                         px[1][k] = {r[0] + r[1], r[3] - r[2]};
                         px[2][k] = {r[4] - r[5], r[6] + r[7]};

@@ -277,6 +277,21 @@ def test_large_phase_path(oracle_mod, idg):
     for variant in VARIANTS:
         vgot = degrid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, spec.n_rows, variant)
         check_rel(f"degridder large-phase v{variant}", vgot, vwant, TOL)
+    # every batched shape on the reduced path
+    from idg_gb300 import tuning
+
+    ng, nd = tuning.num_shapes()
+    saved = tuning.get_shapes(64)
+    for sh in range(max(ng, nd)):
+        tuning.set_shapes(64, min(sh, ng - 1), min(sh, nd - 1))
+        if sh < ng:
+            got = grid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, vis, obs.taper, obs.aterms, L.VARIANT_BATCHED)
+            check_rel(f"gridder large-phase shape {sh}", got, want, TOL)
+        if sh < nd:
+            vgot = degrid_gpu(sp, obs.metadata, obs.uvw, obs.wavenumbers, sub, obs.taper, obs.aterms, spec.n_rows,
+                              L.VARIANT_BATCHED)
+            check_rel(f"degridder large-phase shape {sh}", vgot, vwant, TOL)
+    tuning.set_shapes(64, *saved)
 
 
 def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
