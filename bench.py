@@ -77,7 +77,7 @@ def parse():
     ap.add_argument("--shapes", default="", help="G,D: batched gridder/degridder launch shapes instead of autotuning")
     ap.add_argument("--host-buffers", choices=["auto", "pinned", "hostmem"], default="auto",
                     help="page-locked host buffers of the e2e leg: cudaHostAlloc (pinned), huge-page memory "
-                         "registered with cudaHostRegister (hostmem), or whichever copies faster (auto)")
+                         "registered with cudaHostRegister (hostmem), or whichever runs a trial imaging cycle faster (auto)")
     return ap.parse_args()
 
 
@@ -268,15 +268,17 @@ def copy_probe(host_in, host_out, dev_buf, stream, chunks=32) -> dict:
 
 
 def e2e_host_buffers(kind: str, shape, fill, dev_buf, stream):
-    """The e2e leg's input and output visibility arrays, page-locked.
+    """The e2e leg's candidate input and output visibility arrays, page-locked.
 
     "pinned": cudaHostAlloc (torch pin_memory); "hostmem": transparent-huge-
     page memory registered with cudaHostRegister (idg_gb300.hostmem); "auto":
-    pinned, unless its copy probe runs below 100 GB/s either way and hostmem
-    then probes faster.  The two kinds copy at the same rate on a healthy host
-    (about 210 GB/s in, 190 GB/s out on GB300), but either has been seen to
-    fall well below that in some processes.  Returns (vis_in, vis_out, record);
-    the record names the kind and holds every probe taken."""
+    both, where host memory allows, and the caller keeps the kind whose
+    imaging cycle runs faster.  The two kinds copy at the same rate on a
+    healthy host (about 210 GB/s in, 190 GB/s out on GB300), but cudaHostAlloc
+    memory has been measured well below its own copy probe inside the cycle
+    (39 GB/s in against a 137 GB/s probe), so the choice rests on a cycle and
+    not on the probe.  Returns (candidates, record): candidates maps each kind
+    made to its (vis_in, vis_out) pair; the record holds every probe taken."""
     import torch
 
     from idg_gb300 import hostmem
@@ -292,32 +294,37 @@ def e2e_host_buffers(kind: str, shape, fill, dev_buf, stream):
         copy_probe(a, b, dev_buf, stream)  # first touch of the pages by the copy engines
         return a, b, copy_probe(a, b, dev_buf, stream)
 
-    def drop(k, a, b):
-        if k == "hostmem":
-            hostmem.release(a)
-            hostmem.release(b)
-
-    first = "hostmem" if kind == "hostmem" else "pinned"
-    a, b, pr = make(first)
-    record = {"kind": first, "probes": {first: pr}}
-    room = host_mem_available() > 1.5 * (a.nbytes + b.nbytes)
-    if kind == "auto" and min(pr["h2d_gbs"], pr["d2h_gbs"]) < 100.0 and room:
-        a2, b2, pr2 = make("hostmem")
-        record["probes"]["hostmem"] = pr2
-        if min(pr2.values()) > min(pr.values()):
-            drop(first, a, b)
-            a, b, record["kind"] = a2, b2, "hostmem"
-        else:
-            drop("hostmem", a2, b2)
-    return a, b, record
+    kinds = ["hostmem", "pinned"] if kind == "auto" else [kind]
+    cands, probes = {}, {}
+    for k in kinds:
+        if cands and host_mem_available() < 1.5 * sum(x.nbytes for x in next(iter(cands.values()))):
+            break
+        a, b, pr = make(k)
+        cands[k] = (a, b)
+        probes[k] = pr
+    return cands, {"kind": next(iter(cands)), "probes": probes}
 
 
 def release_host_buffers(record, *arrays):
+    """Unregisters host arrays of the record's kind when they are hostmem
+    arrays (the memory goes with the last reference)."""
     from idg_gb300 import hostmem
 
     if record["kind"] == "hostmem":
         for a in arrays:
             hostmem.release(a)
+
+
+def free_pinned_cache():
+    """Returns torch's cached page-locked host blocks that no array holds any
+    more (pinned arrays stay in its cache after their last reference)."""
+    import gc
+
+    import torch
+
+    gc.collect()
+    if hasattr(torch._C, "_host_emptyCache"):
+        torch._C._host_emptyCache()
 
 
 # ---------------------------------------------------------------------------
@@ -396,17 +403,34 @@ def run_ours(args, rank, world, local_rank):
     e2e_n, e2e_rows = e2e_prefix(obs.metadata, spec.n_rows, 2 * C * 32,
                                  0.6 * host_mem_available() / max(1, local_world))
     if not args.no_e2e:
-        vis_host, out_host, host_rec = e2e_host_buffers(args.host_buffers, (e2e_rows,) + tuple(vis.shape[1:]),
-                                                        vis[:e2e_rows], vis_out[:e2e_rows], stream)
+        cands, host_rec = e2e_host_buffers(args.host_buffers, (e2e_rows,) + tuple(vis.shape[1:]),
+                                           vis[:e2e_rows], vis_out[:e2e_rows], stream)
         chunk = -1  # IDG_CHUNKS_AUTO: gridding chunks growing, degridding chunks shrinking
         aterms_np = hostmem.pinned_copy(obs.aterms)
         md_e2e = hostmem.pinned_copy(obs.metadata[:e2e_n])
         uvw_e2e = hostmem.pinned_copy(obs.uvw[:e2e_rows])
         small = [aterms_np, md_e2e, uvw_e2e]
         nvis_e2e = int(md_e2e["nr_timesteps"].astype(np.int64).sum()) * C
-        for _ in range(2):  # warm: allocates the cycle's device buffers
-            ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, vis_host, obs.taper, aterms_np, out_host,
-                              variant=variant, chunk_subgrids=chunk)
+
+        def cycle(pair):
+            return ops.imaging_cycle(gs, md_e2e, uvw_e2e, obs.wavenumbers, pair[0], obs.taper, aterms_np, pair[1],
+                                     variant=variant, chunk_subgrids=chunk)
+
+        cycle(next(iter(cands.values())))  # warm: allocates the cycle's device buffers
+        trial = {}
+        for kind, pair in cands.items():  # one cycle per kind of host buffer; the faster one is kept
+            t = cycle(pair)
+            trial[kind] = {"ms": round(float(t["total_ms"]), 1),
+                           "h2d_gbs": round(t["h2d_vis_bytes"] / (t["h2d_vis_ms"] * 1e-3) / 1e9, 1)}
+        best = min(trial, key=lambda kd: trial[kd]["ms"])
+        for kind in [kd for kd in cands if kd != best]:
+            pair = cands.pop(kind)
+            release_host_buffers({"kind": kind}, *pair)
+            del pair
+            free_pinned_cache()
+        vis_host, out_host = cands.pop(best)
+        host_rec["kind"] = best
+        cycle((vis_host, out_host))
         totals = []
         if dist:
             dist.barrier()
@@ -425,6 +449,7 @@ def run_ours(args, rank, world, local_rank):
                "ms_per_step": e2e_ms,
                "api": "idg_imaging_cycle (C ABI) on page-locked host buffers",
                "host_buffers": host_rec["kind"],
+               "host_buffer_trial": trial,
                "copy_probe_gbs": host_rec["probes"],
                "h2d_gbs_steps": [round(t["h2d_vis_bytes"] / (t["h2d_vis_ms"] * 1e-3) / 1e9, 1) for t in totals],
                "d2h_gbs_steps": [round(t["d2h_vis_bytes"] / (t["d2h_vis_ms"] * 1e-3) / 1e9, 1) for t in totals],
@@ -441,6 +466,7 @@ def run_ours(args, rank, world, local_rank):
             hostmem.release(a)
         release_host_buffers(host_rec, out_host)
         del out_host, aterms_np, md_e2e, uvw_e2e, small
+        free_pinned_cache()
     elif rank == 0 and not args.skip_cpu:
         vis_host = vis[:e2e_rows].cpu().numpy()
 
