@@ -50,9 +50,9 @@ FLOP_PER_PIXVIS = 34.0  # 16 FMA of the four complex MACs + 1 FMA of the phase
 # DRAM bytes (read + write) per subgrid of one batched kernel launch, S = 32, 16
 # channels x 128 timesteps: ncu capture of one launch on the first 8192
 # subgrids of the config-2 plan with the tuned mirror-quad shapes (gridder
-# shape 22: 690.9 MB read + 246.2 MB written; degridder shape 34: 418.8 MB
+# shape 24: 690.4 MB read + 245.2 MB written; degridder shape 34: 418.4 MB
 # read + 490.1 MB written), divided by 8192.
-DRAM_BYTES_PER_SUBGRID = {"gridder": 114392.0, "degridder": 110950.0}
+DRAM_BYTES_PER_SUBGRID = {"gridder": 114213.0, "degridder": 110901.0}
 
 
 def parse():
