@@ -51,6 +51,28 @@ def make_observation(rng, max_vis: float):
     return spec, grid_job, degrid_job
 
 
+def host_copy_gbs(observations, repeats: int = 3) -> dict:
+    """Copy rates (GB/s) of the jobs' page-locked visibility buffers just before
+    a stream: the first observation's input array to the device and back,
+    `repeats` times each way, best taken.  Job latencies include these copies,
+    so the serving line carries the rate they ran at."""
+    src = observations[0][1].vis
+    dev = torch.empty_like(src, device="cuda")
+    rates = {}
+    for name, dst, frm in (("h2d_gbs", dev, src), ("d2h_gbs", src, dev)):
+        best = 0.0
+        for _ in range(repeats):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(frm, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = max(best, src.numel() * src.element_size() / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+        rates[name] = round(best, 1)
+    del dev
+    return rates
+
+
 def run_stream(observations, rate: float, slots: int = 4, budget_gb: float = 96.0, seed: int = 5) -> dict:
     """Serve the gridding and degridding jobs of `observations` as one Poisson
     stream of mean rate `rate` jobs/s; returns the latency / throughput line.
@@ -58,6 +80,7 @@ def run_stream(observations, rate: float, slots: int = 4, budget_gb: float = 96.
     the stream (into a grid of their own) so that the server's one-time set-up
     is not timed; the percentiles are over the stream's jobs (linear
     interpolation between order statistics)."""
+    copy_rates = host_copy_gbs(observations)
     with Server(max_slots=slots, hbm_budget_bytes=int(budget_gb * (1 << 30)), cta_share=True) as srv:
         spec0, gjob0, djob0 = observations[0]
         warm = srv.grid_create(spec0.grid_size)
@@ -94,6 +117,7 @@ def run_stream(observations, rate: float, slots: int = 4, budget_gb: float = 96.
         "budget_gb": budget_gb,
         "visibilities": nvis,
         "wall_s": st["wall_s"],
+        "host_copy_gbs": copy_rates,
     }
 
 
