@@ -184,6 +184,19 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         row0[s] = a;
         row1[s] = a + m.nr_timesteps;
     }
+    // rows that no entry names (zeroed in the output instead of degridded)
+    std::vector<std::pair<int64_t, int64_t>> gaps;
+    {
+        std::vector<std::pair<int64_t, int64_t>> spans(nr_subgrids);
+        for (int64_t s = 0; s < nr_subgrids; ++s) spans[s] = {row0[s], row1[s]};
+        std::sort(spans.begin(), spans.end());
+        int64_t covered = 0;
+        for (const auto &sp : spans) {
+            if (sp.first > covered) gaps.push_back({covered, sp.first});
+            covered = std::max(covered, sp.second);
+        }
+        if (covered < nr_rows) gaps.push_back({covered, nr_rows});
+    }
     std::vector<Chunk> gch, dch;
     if (!make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, true), row0, row1, &gch) ||
         !make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, false), row0, row1, &dch)) {
@@ -315,8 +328,11 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     }
     IDG_CUDA(cudaEventRecord(t_grid1, B.s_compute));
 
-    // degridding phase (rows the plan does not name come back as zeros)
-    IDG_CUDA(cudaMemsetAsync(B.vis_out, 0, b_vis, B.s_compute));
+    // degridding phase: the degridder writes every row a plan entry names;
+    // the rows no entry names come back as zeros
+    for (const auto &gap : gaps)
+        IDG_CUDA(cudaMemsetAsync(static_cast<char *>(B.vis_out) + (size_t)gap.first * C * 32, 0,
+                                 (size_t)(gap.second - gap.first) * C * 32, B.s_compute));
     for (size_t i = 0; i < dch.size(); ++i) {
         const int64_t s0 = dch[i].s0, n = dch[i].s1 - s0;
         if (int rc = idg_degrid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,

@@ -522,6 +522,45 @@ def test_host_buffer_cycle_matches_device_steps(idg, chunk, locked):
             hostmem.release(a)
 
 
+def test_host_buffer_cycle_zeroes_rows_no_entry_names(idg):
+    """A plan that names only some of the rows (every third config-1 subgrid
+    dropped): idg_imaging_cycle writes the degridded rows and zeros exactly in
+    the rows no entry names, whatever the output buffer held before."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    spec = D.config1()
+    obs = D.make_observation(spec)
+    vis = _vis(spec, seed=43)
+    keep = np.arange(spec.n_subgrids) % 3 != 1
+    md = np.ascontiguousarray(obs.metadata[keep])
+    S, G, N = spec.subgrid_size, spec.grid_size, int(keep.sum())
+    gs = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    d = {k: dev(v) for k, v in dict(md=md, uvw=obs.uvw, k=obs.wavenumbers, vis=vis, taper=obs.taper,
+                                    at=obs.aterms).items()}
+    sub = torch.empty((N, 4, S, S), dtype=torch.complex64, device="cuda")
+    g_ref = torch.zeros((1, 4, G, G), dtype=torch.complex64, device="cuda")
+    ops.grid_visibilities(gs, d["md"], d["uvw"], d["k"], d["vis"], d["taper"], d["at"], sub, g_ref)
+    v_ref = torch.zeros_like(d["vis"])
+    ops.degrid_visibilities(gs, d["md"], d["uvw"], d["k"], v_ref, d["taper"], d["at"], sub, g_ref)
+    torch.cuda.synchronize()
+    named = np.zeros(vis.shape[0], bool)
+    b0 = int(md["baseline_offset"][0])
+    for m in md:
+        r = int(m["baseline_offset"]) - b0 + int(m["time_offset"])
+        named[r:r + int(m["nr_timesteps"])] = True
+    assert named.any() and not named.all()
+    out_h = np.full(vis.shape, np.nan + 1j * np.nan, np.complex64)
+    try:
+        t = ops.imaging_cycle(gs, md, obs.uvw, obs.wavenumbers, vis, obs.taper, np.ascontiguousarray(obs.aterms),
+                              out_h, chunk_subgrids=L.CHUNKS_AUTO)
+        assert np.all(out_h[~named] == 0)
+        check_rel("host cycle vis, rows named", out_h[named], v_ref.cpu().numpy()[named], TOL)
+        assert t["total_ms"] > 0
+    finally:
+        ops.release_buffers()
+
+
 def test_degenerate_plan_entries_every_batched_shape(oracle_mod, idg):
     """Every batched launch shape on plan entries at the edges of what a plan may
     hold: zero and one timestep, empty and one-channel ranges, ranges starting
