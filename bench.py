@@ -480,13 +480,11 @@ def run_ours(args, rank, world, local_rank):
         if ev: ev[2].record(stream)
         bins.add(sub, grid, stream=stream)
         if ev: ev[3].record(stream)
-        # degridding step
-        ops.splitter(gs, md, grid, sub, stream=stream)
+        # degridding step: splitter and backward FFT in one pass, then the degridder
+        ops.split_subgrid_fft(gs, md, grid, sub, taper, stream=stream)
         if ev: ev[4].record(stream)
-        ops.subgrid_fft(gs, sub, -1, taper, stream=stream)
-        if ev: ev[5].record(stream)
         ops.degridder(nogrid, md, uvw, k, vis_out, None, at, sub, variant=v, stream=stream)
-        if ev: ev[6].record(stream)
+        if ev: ev[5].record(stream)
 
     # The batched form runs as one captured CUDA graph per cycle over a device-resident
     # plan (longest-first work list, tuned launch shapes); the plain form as direct calls.
@@ -536,17 +534,17 @@ def run_ours(args, rank, world, local_rank):
 
     # per-kernel times of the same kernels (direct calls, events between launches)
     # for the roofline: one instrumented cycle after the timed region
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
     with torch.cuda.stream(stream):
         step(ev=ev)
     stream.synchronize()
-    parts = np.array([[ev[j].elapsed_time(ev[j + 1]) for j in range(6)]])
+    parts = np.array([[ev[j].elapsed_time(ev[j + 1]) for j in range(5)]])
 
     # roofline (FP32 FMA bound) of the gridder and the degridder; the JSON's
     # top-level figures are those of the kernel with the larger time share
     pixvis = float(nvis) * S * S
     grid_ms = float(np.mean(parts[:, 0]))
-    degrid_ms = float(np.mean(parts[:, 5]))
+    degrid_ms = float(np.mean(parts[:, 4]))
     peak = ops.measure_fp32_peak()
     per_kernel = {}
     for name, ms in (("gridder", grid_ms), ("degridder", degrid_ms)):
@@ -581,7 +579,7 @@ def run_ours(args, rank, world, local_rank):
         "gridder": per_kernel["gridder"],
         "degridder": per_kernel["degridder"],
         "kernel_ms": {n: float(np.mean(parts[:, j])) for j, n in enumerate(
-            ["gridder", "fft_fwd", "adder", "splitter", "fft_bwd", "degridder"])},
+            ["gridder", "fft_fwd", "adder", "split_fft_bwd", "degridder"])},
     }
     if plan is not None:
         plan.close()
@@ -617,12 +615,12 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_plain and variant != ops.VARIANT_PLAIN:
         with torch.cuda.stream(stream):
             step(v=ops.VARIANT_PLAIN)
-            pe = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
+            pe = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
             step(v=ops.VARIANT_PLAIN, ev=pe)
         stream.synchronize()
-        pms = pe[0].elapsed_time(pe[6])
+        pms = pe[0].elapsed_time(pe[5])
         plain = {"value": nvis / (pms * 1e-3) / 1e6, "unit": "Mvis/s", "ms_per_step": pms,
-                 "gridder_ms": pe[0].elapsed_time(pe[1]), "degridder_ms": pe[5].elapsed_time(pe[6])}
+                 "gridder_ms": pe[0].elapsed_time(pe[1]), "degridder_ms": pe[4].elapsed_time(pe[5])}
 
     # serving: Poisson streams of gridding and degridding jobs of mixed sizes,
     # one per arrival rate, over the same observations

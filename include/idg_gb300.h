@@ -205,6 +205,13 @@ IDG_API int idg_adder_binned(const idg_tile_bins *bins, const void *subgrids, vo
  * adder's mirror rule for -W <= z < 0. */
 IDG_API int idg_splitter(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
                          const void *grid, void *subgrids, void *stream);
+/* The splitter and the backward subgrid FFT (direction -1, with `spheroidal`
+ * or NULL) in one pass: the same subgrids, bit for bit, as idg_splitter
+ * followed by idg_subgrid_fft, without writing and reading them in between.
+ * subgrids must be 16-byte aligned.  idg_degrid_visibilities, plans and the
+ * server's degridding jobs use it. */
+IDG_API int idg_split_subgrid_fft(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                                  const void *grid, const float *spheroidal, void *subgrids, void *stream);
 
 /* In-place 2-D FFT of every plane of grid[W][4][G][G] (G a power of two,
  * 64 <= G <= 8192), the imaging step around the path:

@@ -275,6 +275,25 @@ IDG_API int idg_splitter(const idg_params *params, int64_t nr_subgrids, const id
     return IDG_OK;
 }
 
+IDG_API int idg_split_subgrid_fft(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,
+                                  const void *grid, const float *spheroidal, void *subgrids, void *stream) {
+    if (!params) return fail(IDG_ERR_INVALID_ARGUMENT, "params is NULL");
+    if (!fft_size_supported(params->subgrid_size))
+        return fail(IDG_ERR_UNSUPPORTED, "subgrid_size %d: the subgrid FFT supports 8, 16, 24, 32, 48, 64",
+                    params->subgrid_size);
+    if (params->grid_size < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "bad sizes");
+    if (nr_subgrids < 0 || nr_subgrids > INT32_MAX) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_subgrids");
+    if (nr_subgrids == 0) return IDG_OK;
+    if (!metadata || !subgrids || !grid) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    if (!aligned16(subgrids)) return fail(IDG_ERR_INVALID_ARGUMENT, "subgrids must be 16-byte aligned");
+    cudaError_t e = launch_split_fft(metadata, nr_subgrids, params->subgrid_size, params->grid_size,
+                                     params->nr_w_planes > 0 ? params->nr_w_planes : 1,
+                                     reinterpret_cast<const float2 *>(grid), reinterpret_cast<float2 *>(subgrids),
+                                     spheroidal, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "split + subgrid fft launch");
+    return IDG_OK;
+}
+
 IDG_API int idg_grid_fft(const idg_params *params, void *grid, int direction, const float *correction,
                          void *stream) {
     if (!params) return fail(IDG_ERR_INVALID_ARGUMENT, "params is NULL");

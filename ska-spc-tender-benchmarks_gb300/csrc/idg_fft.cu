@@ -16,6 +16,13 @@
 // padded shared memory; one thread per row runs a register-resident radix-2
 // (x radix-3 for S = 24, 48) FFT, then one thread per column does the same,
 // and the planes are stored back with 16-byte stores.
+//
+// Split + backward FFT (SPLIT): the degridding step's splitter and backward
+// FFT in one pass.  The load stage reads each plane's footprint on the uv-grid
+// (the splitter's rule: w-plane z, or the Hermitian mirror -z-1 with
+// coordinates G - (x, y), polarisations 1 and 2 swapped and the value
+// conjugated, for z < 0; zeros outside the grid or the planes) instead of a
+// subgrid, so the subgrid is written once, already in the image domain.
 #include "idg_device.cuh"
 #include "idg_internal.h"
 
@@ -117,13 +124,28 @@ struct FftShape {
     static constexpr int pitch = S + 1; // float2 per padded row
 };
 
-template <int S, int DIR>
+// Where a plane of the split + FFT kernel comes from on the uv-grid.
+struct PlaneSrc {
+    int64_t base;  // offset of the plane's polarisation in the grid, -1: all zeros
+    int x0, y0;    // grid coordinates of pixel (0, 0); mirrored planes step backwards
+    int mirror;
+};
+
+struct SplitArgs {
+    const idg_metadata *md;
+    const float2 *grid;
+    int G, W;
+};
+
+template <int S, int DIR, bool SPLIT>
 __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float2 *data, int64_t nr_planes,
-                                                                          const float *taper) {
+                                                                          const float *taper, SplitArgs sa) {
+    static_assert(!SPLIT || DIR < 0, "the split pass runs before the backward transform");
     using Sh = FftShape<S>;
     __shared__ float2 tw[S];      // e^{+2 pi i m / S}
     __shared__ float2 post[S];    // c_j = (-1)^j e^{+i pi (j - S/2)/S}
     __shared__ float2 buf[Sh::planes][S][Sh::pitch];
+    __shared__ PlaneSrc src_of[SPLIT ? Sh::planes : 1];
     constexpr int kBatch = 8;     // 16-byte loads in flight per thread
 
     const int tid = threadIdx.x;
@@ -139,6 +161,20 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
     }
     const int64_t plane0 = (int64_t)blockIdx.x * Sh::planes;
     const int nplanes = (int)min((int64_t)Sh::planes, nr_planes - plane0);
+    if (SPLIT && tid < nplanes) {
+        const int64_t p = plane0 + tid;
+        const idg_metadata m = sa.md[p >> 2];
+        const int pol = (int)(p & 3);
+        const bool ok = m.z >= -sa.W && m.z < sa.W, mirror = m.z < 0;
+        const int pg = (mirror && (pol == 1 || pol == 2)) ? 3 - pol : pol;
+        const int64_t w = ok ? (mirror ? -m.z - 1 : m.z) : 0;
+        PlaneSrc ps;
+        ps.base = ok ? (w * 4 + pg) * (int64_t)sa.G * sa.G : -1;
+        ps.x0 = mirror ? sa.G - m.x : m.x;
+        ps.y0 = mirror ? sa.G - m.y : m.y;
+        ps.mirror = mirror;
+        src_of[tid] = ps;
+    }
     __syncthreads();
 
     // load + pre-multiply: two complex values per 16-byte load, a batch of
@@ -150,7 +186,29 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
 #pragma unroll
         for (int k = 0; k < kBatch; ++k) {
             const int e2 = base + tid + k * Sh::threads;
-            v[k] = e2 < total2 ? src[e2] : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!SPLIT) {
+                v[k] = e2 < total2 ? src[e2] : make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                // two neighbouring pixels of one plane's row, each read from the grid
+                v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (e2 < total2) {
+                    const int e = 2 * e2, pl = e / (S * S), q = e - pl * S * S, y = q / S, x = q - y * S;
+                    const PlaneSrc ps = src_of[pl];
+                    const int step = ps.mirror ? -1 : 1;
+                    const int gy = ps.y0 + step * y, gx = ps.x0 + step * x;
+                    if (ps.base >= 0 && gy >= 0 && gy < sa.G) {
+                        const float2 *row = sa.grid + ps.base + (int64_t)gy * sa.G;
+                        float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+                        if (gx >= 0 && gx < sa.G) a = __ldg(row + gx);
+                        if (gx + step >= 0 && gx + step < sa.G) b = __ldg(row + gx + step);
+                        if (ps.mirror) {
+                            a.y = -a.y;
+                            b.y = -b.y;
+                        }
+                        v[k] = make_float4(a.x, a.y, b.x, b.y);
+                    }
+                }
+            }
         }
 #pragma unroll
         for (int k = 0; k < kBatch; ++k) {
@@ -223,10 +281,22 @@ cudaError_t launch_fft_s(float2 *data, int64_t nr_planes, int direction, const f
     using Sh = FftShape<S>;
     const int64_t blocks = (nr_planes + Sh::planes - 1) / Sh::planes;
     if (blocks == 0) return cudaSuccess;
+    const SplitArgs none{nullptr, nullptr, 0, 0};
     if (direction > 0)
-        subgrid_fft_kernel<S, 1><<<(unsigned)blocks, Sh::threads, 0, stream>>>(data, nr_planes, taper);
+        subgrid_fft_kernel<S, 1, false><<<(unsigned)blocks, Sh::threads, 0, stream>>>(data, nr_planes, taper, none);
     else
-        subgrid_fft_kernel<S, -1><<<(unsigned)blocks, Sh::threads, 0, stream>>>(data, nr_planes, taper);
+        subgrid_fft_kernel<S, -1, false><<<(unsigned)blocks, Sh::threads, 0, stream>>>(data, nr_planes, taper, none);
+    return cudaGetLastError();
+}
+
+template <int S>
+cudaError_t launch_split_fft_s(const idg_metadata *md, int64_t nr_planes, int G, int W, const float2 *grid,
+                               float2 *subgrids, const float *taper, cudaStream_t stream) {
+    using Sh = FftShape<S>;
+    const int64_t blocks = (nr_planes + Sh::planes - 1) / Sh::planes;
+    if (blocks == 0) return cudaSuccess;
+    const SplitArgs sa{md, grid, G, W};
+    subgrid_fft_kernel<S, -1, true><<<(unsigned)blocks, Sh::threads, 0, stream>>>(subgrids, nr_planes, taper, sa);
     return cudaGetLastError();
 }
 
@@ -244,6 +314,20 @@ cudaError_t launch_subgrid_fft(float2 *data, int64_t nr_subgrids, int S, int dir
     case 32: return launch_fft_s<32>(data, planes, direction, taper, stream);
     case 48: return launch_fft_s<48>(data, planes, direction, taper, stream);
     case 64: return launch_fft_s<64>(data, planes, direction, taper, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_split_fft(const idg_metadata *md, int64_t nr_subgrids, int S, int G, int W, const float2 *grid,
+                             float2 *subgrids, const float *taper, cudaStream_t stream) {
+    const int64_t planes = nr_subgrids * 4;
+    switch (S) {
+    case 8: return launch_split_fft_s<8>(md, planes, G, W, grid, subgrids, taper, stream);
+    case 16: return launch_split_fft_s<16>(md, planes, G, W, grid, subgrids, taper, stream);
+    case 24: return launch_split_fft_s<24>(md, planes, G, W, grid, subgrids, taper, stream);
+    case 32: return launch_split_fft_s<32>(md, planes, G, W, grid, subgrids, taper, stream);
+    case 48: return launch_split_fft_s<48>(md, planes, G, W, grid, subgrids, taper, stream);
+    case 64: return launch_split_fft_s<64>(md, planes, G, W, grid, subgrids, taper, stream);
     default: return cudaErrorInvalidValue;
     }
 }

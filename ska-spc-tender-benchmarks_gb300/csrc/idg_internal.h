@@ -32,6 +32,10 @@ void set_batched_degridder_shape(int S, int shape);
 bool fft_size_supported(int S);
 cudaError_t launch_subgrid_fft(float2 *data, int64_t nr_subgrids, int S, int direction, const float *taper,
                                cudaStream_t stream);
+// The degridding step's splitter and backward subgrid FFT in one pass (same
+// result as launch_splitter followed by launch_subgrid_fft with direction -1).
+cudaError_t launch_split_fft(const struct idg_metadata *md, int64_t nr_subgrids, int S, int G, int W,
+                             const float2 *grid, float2 *subgrids, const float *taper, cudaStream_t stream);
 
 bool grid_fft_size_supported(int G);
 cudaError_t launch_grid_fft(float2 *grid, int G, int planes, int direction, const float *correction,

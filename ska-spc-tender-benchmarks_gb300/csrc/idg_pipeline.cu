@@ -144,8 +144,18 @@ IDG_API int idg_degrid_visibilities(const idg_params *params, int variant, int64
                                     void *stream) {
     if (int rc = check_step_args(params, nr_subgrids, subgrids, grid)) return rc;
     if (nr_subgrids == 0) return IDG_OK;
-    if (int rc = idg_splitter(params, nr_subgrids, metadata, grid, subgrids, stream)) return rc;
-    if (int rc = idg_subgrid_fft(params, nr_subgrids, -1, spheroidal, subgrids, stream)) return rc;
+    if (!fft_size_supported(params->subgrid_size))
+        return fail(IDG_ERR_UNSUPPORTED, "subgrid_size %d: the subgrid FFT supports 8, 16, 24, 32, 48, 64",
+                    params->subgrid_size);
+    if (!metadata) return fail(IDG_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    if (reinterpret_cast<uintptr_t>(subgrids) % 16 != 0)
+        return fail(IDG_ERR_INVALID_ARGUMENT, "subgrids must be 16-byte aligned");
+    // splitter and backward subgrid FFT in one pass
+    cudaError_t e = launch_split_fft(metadata, nr_subgrids, params->subgrid_size, params->grid_size,
+                                     params->nr_w_planes > 0 ? params->nr_w_planes : 1,
+                                     static_cast<const float2 *>(grid), static_cast<float2 *>(subgrids), spheroidal,
+                                     reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "split + subgrid fft launch");
     idg_params p = *params;
     p.flags |= IDG_FLAG_NO_TAPER;
     return idg_degridder(&p, variant, nr_subgrids, metadata, ext, nr_rows, uvw, wavenumbers, visibilities, nullptr,

@@ -118,12 +118,11 @@ int grid_step(idg_plan *p, const float *uvw, const float *k, const void *vis, co
 int degrid_step(idg_plan *p, const float *uvw, const float *k, void *vis_out, const float *taper, const void *aterms,
                 const void *grid, cudaStream_t st) {
     const idg_params &q = p->params;
-    cudaError_t e = launch_splitter(p->d_md, p->nr_subgrids, q.subgrid_size, q.grid_size,
-                                    q.nr_w_planes > 0 ? q.nr_w_planes : 1, reinterpret_cast<const float2 *>(grid),
-                                    reinterpret_cast<float2 *>(p->d_subgrids), st);
-    if (e != cudaSuccess) return cuda_fail(e, "plan splitter");
-    e = launch_subgrid_fft(reinterpret_cast<float2 *>(p->d_subgrids), p->nr_subgrids, q.subgrid_size, -1, taper, st);
-    if (e != cudaSuccess) return cuda_fail(e, "plan subgrid fft");
+    // splitter and backward subgrid FFT in one pass
+    cudaError_t e = launch_split_fft(p->d_md, p->nr_subgrids, q.subgrid_size, q.grid_size,
+                                     q.nr_w_planes > 0 ? q.nr_w_planes : 1, reinterpret_cast<const float2 *>(grid),
+                                     reinterpret_cast<float2 *>(p->d_subgrids), taper, st);
+    if (e != cudaSuccess) return cuda_fail(e, "plan split + subgrid fft");
     if (p->variant == IDG_VARIANT_BATCHED)
         IDG_CUDA(cudaMemsetAsync(reinterpret_cast<int *>(p->d_words) + 1, 0, sizeof(int), st));
     KernelArgs a = plan_args(p, uvw, k, taper, aterms, vis_out, p->d_subgrids, true);

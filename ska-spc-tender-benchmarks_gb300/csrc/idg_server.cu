@@ -265,9 +265,8 @@ void idg_server::launch(Job &j) {
         if (j.add_done) chk(cudaEventRecord(j.add_done, st));
         g.last_add = j.add_done ? j.add_done : j.done;
     } else {
-        chk(launch_splitter(a.md, (int64_t)N, p.subgrid_size, p.grid_size, g.planes,
-                            static_cast<const float2 *>(g.dev), a.subgrids, st));
-        chk(launch_subgrid_fft(a.subgrids, (int64_t)N, p.subgrid_size, -1, a.taper, st));
+        chk(launch_split_fft(a.md, (int64_t)N, p.subgrid_size, p.grid_size, g.planes,
+                             static_cast<const float2 *>(g.dev), a.subgrids, a.taper, st));
         chk(launch_degridder(a, variant, p.nr_channels, st));
     }
     if (j.k1) chk(cudaEventRecord(j.k1, st));

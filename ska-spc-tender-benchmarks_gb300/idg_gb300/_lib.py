@@ -203,6 +203,7 @@ _SIGNATURES = {
     "idg_subgrid_fft": [ctypes.POINTER(IdgParams), _I64, _I32, _P, _P, _P],
     "idg_adder": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
     "idg_splitter": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P],
+    "idg_split_subgrid_fft": [ctypes.POINTER(IdgParams), _I64, _P, _P, _P, _P, _P],
     "idg_tile_bins_create": [ctypes.POINTER(IdgParams), _I64, _P, ctypes.POINTER(ctypes.c_void_p)],
     "idg_tile_bins_destroy": [_P],
     "idg_tile_bins_info": [_P, ctypes.POINTER(ctypes.c_int64)],

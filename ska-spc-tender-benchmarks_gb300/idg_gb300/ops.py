@@ -194,6 +194,20 @@ def splitter(spec: GridSpec, metadata, grid, subgrids, stream=None):
     return subgrids
 
 
+def split_subgrid_fft(spec: GridSpec, metadata, grid, subgrids, taper=None, stream=None):
+    """splitter followed by subgrid_fft(-1, taper), in one pass over the data."""
+    S, G, W = spec.subgrid_size, spec.grid_size, spec.nr_w_planes
+    _req(metadata, "metadata", torch.int32)
+    _req(subgrids, "subgrids", torch.complex64, (metadata.shape[0], 4, S, S))
+    _req(grid, "grid", torch.complex64, (W, 4, G, G))
+    if taper is not None:
+        _req(taper, "taper", torch.float32, (S, S))
+    p = spec.to_c()
+    _lib.call("idg_split_subgrid_fft", ctypes.byref(p), metadata.shape[0], ptr(metadata), ptr(grid), ptr(taper),
+              ptr(subgrids), _stream_handle(stream))
+    return subgrids
+
+
 def grid_fft(spec: GridSpec, grid, direction: int, correction=None, stream=None):
     """In-place 2-D FFT of every plane of grid[W,4,G,G] (idg_grid_fft): direction -1
     uv -> image with the grid correction applied after, +1 image -> uv with it before."""

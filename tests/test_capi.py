@@ -77,6 +77,11 @@ def test_argument_errors_before_device_work(idg):
     p40 = _lib.IdgParams(1024, 40, 16, 4, 1, 1, 0.1, 0.0, 0, 0)
     assert lib.idg_subgrid_fft(ctypes.byref(p40), 1, 1, None, None, None) == _lib.IDG_ERR_UNSUPPORTED
     assert lib.idg_subgrid_fft(ctypes.byref(p), 1, 0, None, None, None) == _lib.IDG_ERR_INVALID_ARGUMENT
+    # splitter + backward FFT in one pass: FFT sizes, counts and pointers checked first
+    assert lib.idg_split_subgrid_fft(ctypes.byref(p40), 1, None, None, None, None, None) == _lib.IDG_ERR_UNSUPPORTED
+    assert lib.idg_split_subgrid_fft(ctypes.byref(p), -1, None, None, None, None, None) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert lib.idg_split_subgrid_fft(ctypes.byref(p), 1, None, None, None, None, None) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert lib.idg_split_subgrid_fft(ctypes.byref(p), 0, None, None, None, None, None) == _lib.IDG_OK
     # launcher config
     cfg = _lib.IdgLaunchConfig(0, 1024, 32, 4, 16, 1, 32, 0.1, 0.0, 0, 0)
     r = _lib.IdgBenchmarkResult()

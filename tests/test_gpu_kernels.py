@@ -168,6 +168,40 @@ def test_adder_splitter_vs_oracle(oracle_mod, idg):
     assert np.array_equal(out.cpu().numpy(), oracle_mod.splitter(g, md, S).astype(np.complex64))
 
 
+@pytest.mark.parametrize("S", [8, 24, 32, 64])
+def test_split_fft_pass_equals_splitter_then_fft(idg, S):
+    """The degridding step reads the grid and runs the backward subgrid FFT in
+    one pass: its subgrids equal the splitter followed by the backward FFT bit
+    for bit, with w-planes, mirrored negative-w entries, entries outside the
+    planes and footprints partly or wholly outside the grid."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    spec = D.config1()
+    spec.subgrid_size = S
+    obs = D.make_observation(spec)
+    G, W, N = 160, 2, spec.n_subgrids
+    rng = np.random.default_rng(S)
+    md = obs.metadata.copy()
+    md["x"] = rng.integers(-S + 2, G - 2, N)
+    md["y"] = rng.integers(-S + 2, G - 2, N)
+    md["z"] = rng.integers(-W, W, N)
+    md["x"][:4] = [-S, G, G - S // 2 - 1, -S // 2 + 1]  # wholly outside / straddling the edges
+    md["z"][4], md["z"][5] = W, -W - 1                   # outside the planes: zeros
+    assert (md["z"] < 0).sum() >= 4
+    sp = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size, W=W)
+    g = dev((rng.standard_normal((W, 4, G, G)) + 1j * rng.standard_normal((W, 4, G, G))).astype(np.complex64))
+    d = {k: dev(v) for k, v in dict(md=md, uvw=obs.uvw, k=obs.wavenumbers, taper=obs.taper, at=obs.aterms).items()}
+    want = torch.empty((N, 4, S, S), dtype=torch.complex64, device="cuda")
+    ops.splitter(sp, d["md"], g, want)
+    ops.subgrid_fft(sp, want, -1, d["taper"])
+    got = torch.empty_like(want)
+    vis = torch.zeros((obs.uvw.shape[0], spec.nchannels, 4), dtype=torch.complex64, device="cuda")
+    ops.degrid_visibilities(sp, d["md"], d["uvw"], d["k"], vis, d["taper"], d["at"], got, g)
+    torch.cuda.synchronize()
+    assert np.array_equal(got.cpu().numpy(), want.cpu().numpy())
+
+
 def test_bad_plan_entry_is_flagged_not_faulted(idg):
     from idg_gb300 import ops
 
