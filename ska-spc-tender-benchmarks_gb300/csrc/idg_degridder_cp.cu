@@ -800,6 +800,10 @@ __global__ void __maxnreg__(MAXR) degridder_quad_kernel_r(KernelArgs a) {
 // operands (128 registers) would not fit beside the accumulators.  Forming
 // the factors two channel pairs at a time (operands read twice) needs as many
 // registers, and at 12 warps per SM both forms spill heavily.
+// On GB300 at S = 32 the octets run within 1 % of the column-form quads: the
+// five sincos per octet and channel pair keep the SFU pipe about half busy,
+// where a column run of quads needs 2.25 per quad.  The autotuner picks
+// between them per subgrid size.
 // ---------------------------------------------------------------------------
 // 512 B of operands per octet padded to 528 B: the four lanes of a group read
 // octets 132 words = 4 banks apart.
