@@ -72,6 +72,8 @@ struct Job {
     cudaEvent_t add_done = nullptr;         // gridding jobs: after the adder
     TileBinsHost bins;                      // gridding jobs: the adder's tile bins
     double dev_start_ms = -1, dev_end_ms = -1; // k0, k1 relative to the server's epoch event
+    double est_ms = 0;                      // estimated device time at the full CTA budget
+    int share = 1;                          // its kernels' share of that budget: 1 / share
     int status = IDG_OK;
     bool finished = false;
 };
@@ -120,6 +122,10 @@ struct idg_server {
     std::map<int64_t, Grid> grids;
     int64_t next_job = 1, next_grid = 1;
     size_t in_use = 0, peak_use = 0;
+    // device milliseconds per 1e9 pixel-visibilities of a job's kernels at the
+    // full CTA budget: a running estimate from the finished jobs (seeded with
+    // GB300's config-2 rate)
+    double ms_per_gpv = 0.6;
     int64_t completed = 0, rejected = 0, failed = 0, total_vis = 0;
     std::vector<double> latencies;
     Clock::time_point first_submit{}, last_done{};
@@ -230,12 +236,21 @@ void idg_server::launch(Job &j) {
     a.work_list = static_cast<const int *>(dp(L.work));
     a.work_counter = static_cast<int *>(dp(L.words));
     a.status = static_cast<unsigned *>(dp(L.words)) + 2;
-    int running = 0;
-    for (auto &s : slots)
-        if (s) ++running;
-    // running jobs share the SMs: each persistent kernel takes 1/running of the
-    // CTAs that would fill the GPU with its own launch shape
-    a.share_den = (cfg.cta_share && running > 1) ? running : 0;
+    // Running jobs share the SMs: a persistent kernel takes 1/share of the
+    // CTAs that would fill the GPU with its own launch shape, and keeps them
+    // to its end.  Peers estimated to finish within a quarter of this job's
+    // own time do not count: the CTAs they free are this job's soon after.
+    const double pixvis = (double)j.nvis * (double)p.subgrid_size * (double)p.subgrid_size;
+    j.est_ms = pixvis * 1e-9 * ms_per_gpv;
+    int share = 1;
+    const Clock::time_point now = Clock::now();
+    for (auto &other : slots) {
+        if (!other || other.get() == &j) continue;
+        const double left = other->est_ms * other->share - ms_between(other->t_admit, now);
+        if (left > 0.25 * j.est_ms) ++share;
+    }
+    j.share = cfg.cta_share ? share : 1;
+    a.share_den = j.share > 1 ? j.share : 0;
     const int variant = j.spec.variant == IDG_VARIANT_PLAIN ? IDG_VARIANT_PLAIN : IDG_VARIANT_BATCHED;
 
     // order against the other jobs on this grid
@@ -349,6 +364,9 @@ void idg_server::poll_locked() {
                 cudaEventElapsedTime(&t1, epoch, j.k1) == cudaSuccess) {
                 j.dev_start_ms = t0;
                 j.dev_end_ms = t1;
+                // the rate estimate: only jobs that ran alone measure the full budget
+                const double gpv = (double)j.nvis * j.spec.params.subgrid_size * j.spec.params.subgrid_size * 1e-9;
+                if (j.share == 1 && gpv > 0.5 && t1 > t0) ms_per_gpv = 0.8 * ms_per_gpv + 0.2 * ((t1 - t0) / gpv);
             } else {
                 cudaGetLastError();
             }

@@ -45,9 +45,15 @@ def make_observation(rng, max_vis: float):
     vis_host = torch.empty(vis.shape, dtype=vis.dtype, pin_memory=True)
     vis_host.copy_(vis)
     out_host = torch.zeros_like(vis_host).pin_memory()
-    aterms = np.ascontiguousarray(obs.aterms)
-    grid_job = JobData(gs, obs.metadata, obs.uvw, obs.wavenumbers, obs.taper, aterms, vis_host)
-    degrid_job = JobData(gs, obs.metadata, obs.uvw, obs.wavenumbers, obs.taper, aterms, out_host)
+    # every host input page-locked, as a serving client keeps them: a copy from
+    # pageable memory runs through a staging buffer at the host's pageable rate
+    # and holds the server's scheduler thread meanwhile
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+
+    uvw, k, taper, aterms = pinned(obs.uvw), pinned(obs.wavenumbers), pinned(obs.taper), pinned(obs.aterms)
+    grid_job = JobData(gs, obs.metadata, uvw, k, taper, aterms, vis_host)
+    degrid_job = JobData(gs, obs.metadata, uvw, k, taper, aterms, out_host)
     return spec, grid_job, degrid_job
 
 

@@ -22,14 +22,16 @@ from .ops import GridSpec
 
 @dataclass
 class JobData:
-    """Host arrays of one job (keep them alive until the job is waited on)."""
+    """Host arrays of one job (keep them alive until the job is waited on):
+    numpy arrays or CPU tensors; page-locked ones (pinned tensors) are copied
+    without a staging pass."""
 
     spec: GridSpec
     metadata: np.ndarray
-    uvw: np.ndarray
-    wavenumbers: np.ndarray
-    taper: np.ndarray
-    aterms: np.ndarray
+    uvw: object
+    wavenumbers: object
+    taper: object
+    aterms: object
     vis: object              # gridding: input; degridding: output buffer (numpy or pinned tensor)
     ext: np.ndarray | None = None
 
