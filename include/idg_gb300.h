@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define IDG_ABI_VERSION 2
+#define IDG_ABI_VERSION 3
 
 typedef enum idg_status {
     IDG_OK = 0,
@@ -387,6 +387,11 @@ typedef struct idg_job_stats {
      * show that their kernels ran on the GPU at the same time. */
     double device_start_ms;
     double device_end_ms;
+    /* The job's whole stream work (its copies in, kernels and copy out), in
+     * the same clock: stream_start_ms .. device_start_ms is the copy in plus
+     * any wait for the grid's other jobs. */
+    double stream_start_ms;
+    double stream_end_ms;
 } idg_job_stats;
 
 typedef struct idg_server_stats {

@@ -69,9 +69,11 @@ struct Job {
     void *arena = nullptr;
     cudaEvent_t done = nullptr;
     cudaEvent_t k0 = nullptr, k1 = nullptr; // around the job's kernels (timing events)
+    cudaEvent_t c0 = nullptr, c1 = nullptr; // around all of its stream work, copies included
     cudaEvent_t add_done = nullptr;         // gridding jobs: after the adder
     TileBinsHost bins;                      // gridding jobs: the adder's tile bins
     double dev_start_ms = -1, dev_end_ms = -1; // k0, k1 relative to the server's epoch event
+    double work_start_ms = -1, work_end_ms = -1; // c0, c1
     double est_ms = 0;                      // estimated device time at the full CTA budget
     int share = 1;                          // its kernels' share of that budget: 1 / share
     int status = IDG_OK;
@@ -188,6 +190,7 @@ void idg_server::launch(Job &j) {
     auto chk = [&](cudaError_t x) {
         if (e == cudaSuccess && x != cudaSuccess) e = x;
     };
+    if (j.c0) chk(cudaEventRecord(j.c0, st));
     chk(cudaMemcpyAsync(dp(L.md), j.md.data(), sizeof(idg_metadata) * N, cudaMemcpyHostToDevice, st));
     if (!j.ext.empty()) chk(cudaMemcpyAsync(dp(L.ext), j.ext.data(), sizeof(idg_subgrid_ext) * N, cudaMemcpyHostToDevice, st));
     chk(cudaMemcpyAsync(dp(L.work), j.work.data(), sizeof(int) * N, cudaMemcpyHostToDevice, st));
@@ -287,6 +290,7 @@ void idg_server::launch(Job &j) {
     if (j.k1) chk(cudaEventRecord(j.k1, st));
     if (j.spec.op == IDG_JOB_DEGRID)
         chk(cudaMemcpyAsync(j.spec.vis_out, dp(L.vis), b_vis, cudaMemcpyDeviceToHost, st));
+    if (j.c1) chk(cudaEventRecord(j.c1, st));
     chk(cudaEventRecord(j.done, st));
     if (g.last_op != j.spec.op) g.holders.clear();
     g.last_op = j.spec.op;
@@ -339,6 +343,11 @@ void idg_server::admit_locked() {
             if (j.k0) cudaEventDestroy(j.k0);
             j.k0 = j.k1 = nullptr; // the job runs without its device interval
         }
+        if (cudaEventCreate(&j.c0) != cudaSuccess || cudaEventCreate(&j.c1) != cudaSuccess) {
+            cudaGetLastError();
+            if (j.c0) cudaEventDestroy(j.c0);
+            j.c0 = j.c1 = nullptr; // ... and without its stream interval
+        }
         launch(j);
         it = queue.erase(it);
         cv_done.notify_all(); // a grid read may be waiting for this job's admission
@@ -371,9 +380,21 @@ void idg_server::poll_locked() {
                 cudaGetLastError();
             }
         }
+        if (j.c0 && j.c1 && q == cudaSuccess && j.status == IDG_OK) {
+            float t0 = 0, t1 = 0;
+            if (cudaEventElapsedTime(&t0, epoch, j.c0) == cudaSuccess &&
+                cudaEventElapsedTime(&t1, epoch, j.c1) == cudaSuccess) {
+                j.work_start_ms = t0;
+                j.work_end_ms = t1;
+            } else {
+                cudaGetLastError();
+            }
+        }
         if (j.k0) cudaEventDestroy(j.k0);
         if (j.k1) cudaEventDestroy(j.k1);
-        j.k0 = j.k1 = nullptr;
+        if (j.c0) cudaEventDestroy(j.c0);
+        if (j.c1) cudaEventDestroy(j.c1);
+        j.k0 = j.k1 = j.c0 = j.c1 = nullptr;
         // plan entries the kernels rejected
         if (j.status == IDG_OK) {
             unsigned st = 0;
@@ -436,6 +457,19 @@ IDG_API int idg_server_create(const idg_server_config *cfg, idg_server **out) {
     cudaGetDevice(&srv->device);
     srv->slots.resize(cfg->max_slots);
     srv->streams.resize(cfg->max_slots);
+    // Job arenas come from the device's default stream-ordered pool.  Keep up
+    // to the budget in it across synchronisations, so that a job's arena is
+    // carved from memory a finished job returned rather than mapped anew
+    // (the pool's default is to give unused memory back at every sync).
+    {
+        cudaMemPool_t pool = nullptr;
+        if (cudaDeviceGetDefaultMemPool(&pool, srv->device) == cudaSuccess) {
+            uint64_t keep = (uint64_t)cfg->hbm_budget_bytes, have = 0;
+            if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &have) == cudaSuccess && have < keep)
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    }
     for (auto &s : srv->streams) {
         cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
@@ -626,6 +660,8 @@ IDG_API int idg_server_wait(idg_server *srv, int64_t job_id, int64_t timeout_ms,
         stats->status = j->status;
         stats->device_start_ms = j->dev_start_ms;
         stats->device_end_ms = j->dev_end_ms;
+        stats->stream_start_ms = j->work_start_ms;
+        stats->stream_end_ms = j->work_end_ms;
     }
     srv->jobs.erase(job_id);
     if (j->status != IDG_OK) return fail(j->status, "job %lld failed", (long long)job_id);

@@ -142,6 +142,8 @@ class IdgJobStats(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("device_start_ms", ctypes.c_double),
         ("device_end_ms", ctypes.c_double),
+        ("stream_start_ms", ctypes.c_double),
+        ("stream_end_ms", ctypes.c_double),
     ]
 
 

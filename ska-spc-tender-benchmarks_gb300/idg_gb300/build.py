@@ -22,8 +22,11 @@ LIB_DIR = os.path.join(PKG_DIR, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libidg_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -ffp-contract=off for the host compiler: host code (the reference data
+# generator, the planners) must give the same bits on x86-64 and on aarch64,
+# where gcc would otherwise fuse a * b + c into one rounding.
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-              "--expt-relaxed-constexpr", "-I", INCLUDE]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", INCLUDE]
 
 
 def nvcc() -> str:

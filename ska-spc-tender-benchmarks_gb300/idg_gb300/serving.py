@@ -119,7 +119,8 @@ class Server:
         _lib.check(rc)
         return {"queue_ms": st.queue_ms, "run_ms": st.run_ms, "latency_ms": st.latency_ms,
                 "visibilities": st.visibilities, "device_start_ms": st.device_start_ms,
-                "device_end_ms": st.device_end_ms}
+                "device_end_ms": st.device_end_ms, "stream_start_ms": st.stream_start_ms,
+                "stream_end_ms": st.stream_end_ms}
 
     def stats(self) -> dict:
         s = IdgServerSummary()

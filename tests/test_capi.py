@@ -44,7 +44,7 @@ def test_library_exports_every_declared_symbol(idg):
     lib = idg.load()
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.idg_abi_version() == 2
+    assert lib.idg_abi_version() == 3
 
 
 def test_library_is_in_tree(idg):
