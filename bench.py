@@ -405,7 +405,7 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_e2e:
         cands, host_rec = e2e_host_buffers(args.host_buffers, (e2e_rows,) + tuple(vis.shape[1:]),
                                            vis[:e2e_rows], vis_out[:e2e_rows], stream)
-        chunk = -1  # IDG_CHUNKS_AUTO: gridding chunks growing, degridding chunks shrinking
+        chunk = -2  # IDG_CHUNKS_ADAPTIVE: gridding chunks growing (ratio from the last cycle), degridding shrinking
         aterms_np = hostmem.pinned_copy(obs.aterms)
         md_e2e = hostmem.pinned_copy(obs.metadata[:e2e_n])
         uvw_e2e = hostmem.pinned_copy(obs.uvw[:e2e_rows])
@@ -456,6 +456,8 @@ def run_ours(args, rank, world, local_rank):
                "host_buffers_gb": round((vis_host.nbytes + out_host.nbytes + sum(x.nbytes for x in small)) / 1e9, 2),
                "subgrids": e2e_n,
                "chunks": {"gridding": int(totals[-1]["grid_chunks"]), "degridding": int(totals[-1]["degrid_chunks"])},
+               "chunk_ratio_steps": [round(t["chunk_ratio"], 3) for t in totals],
+               "gridding_wait_ms_steps": [round(t["gridding_wait_ms"], 1) for t in totals],
                "gridding_ms": float(np.mean([t["gridding_ms"] for t in totals])),
                "degridding_ms": float(np.mean([t["degridding_ms"] for t in totals])),
                "steps_ms": [round(x, 1) for x in steps_ms],

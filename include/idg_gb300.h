@@ -437,10 +437,20 @@ typedef struct idg_cycle_timing {
     int64_t d2h_vis_bytes;
     int64_t grid_chunks;   /* chunks of the gridding phase */
     int64_t degrid_chunks; /* chunks of the degridding phase */
+    /* Time the gridding kernels spent waiting for their chunks' copies in
+     * (within gridding_ms), and the growth ratio of the chunks. */
+    double gridding_wait_ms;
+    double chunk_ratio;
 } idg_cycle_timing;
 
 /* chunk_subgrids of idg_imaging_cycle: chunks sized for the copy pipeline */
 #define IDG_CHUNKS_AUTO (-1)
+/* ... with the growth ratio set from the previous cycle: at most 0.9 x
+ * copy rate / kernel rate, stepped down by 15 % after a cycle whose gridding
+ * kernels waited for copies more than 2 % of the phase and up by 5 % after
+ * one that did not, kept within [1.1, 1.6].  Slower or unevenly arriving
+ * copies get finer chunks.  The first cycle uses 1.6. */
+#define IDG_CHUNKS_ADAPTIVE (-2)
 
 /* One imaging cycle on HOST buffers: copies the plan, uvw, wavenumbers,
  * taper, A-terms and input visibilities in, grids them into a zeroed grid,
@@ -453,7 +463,8 @@ typedef struct idg_cycle_timing {
  * gridding (the first copy in is small, so the kernels start early, and each
  * later copy finishes while the previous chunk is gridded, for copy rates of
  * 1.6x the rate the kernels consume) and shrink by 1.6x while degridding (the
- * last copy out is small), at least 1024 subgrids each; 0: one chunk.  uvw
+ * last copy out is small), at least 1024 subgrids each; IDG_CHUNKS_ADAPTIVE:
+ * the same with the ratio learned from the previous cycle; 0: one chunk.  uvw
  * rows travel with their chunk.  Device buffers are kept between calls of
  * the same sizes and freed by idg_release_buffers().  Pinned host buffers
  * give full copy bandwidth.  The cycle clears the device check word (see

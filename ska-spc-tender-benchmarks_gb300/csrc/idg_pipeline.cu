@@ -33,6 +33,7 @@ struct CycleBuffers {
     void *vis_in = nullptr, *vis_out = nullptr, *subgrids = nullptr, *grid = nullptr;
     size_t b_uvw = 0, b_k = 0, b_taper = 0, b_aterms = 0, b_md = 0, b_vis = 0, b_vis_out = 0, b_sub = 0, b_grid = 0;
     cudaStream_t s_compute = nullptr, s_h2d = nullptr, s_d2h = nullptr;
+    double next_ratio = 1.6; // IDG_CHUNKS_ADAPTIVE: the ratio the next cycle uses
 
     void release() {
         for (void *p : {uvw, k, taper, aterms, md, vis_in, vis_out, subgrids, grid})
@@ -55,25 +56,26 @@ struct Chunk {
 };
 
 // Subgrid boundaries 0 = b0 < b1 < ... = n.  chunk > 0: equal chunks of that
-// many subgrids; IDG_CHUNKS_AUTO: kAutoChunks chunks whose sizes grow by
-// kAutoRatio from one to the next (`growing`) or shrink by it (otherwise),
-// chunks under kMinChunk subgrids merged into their neighbour; anything else:
-// one chunk.  A growing chunk's copy keeps ahead of the previous chunk's
-// kernels while the copy rate is at least kAutoRatio times the rate the
-// kernels consume visibilities (about 61 GB/s for the config-2 gridder:
-// copies at 98 GB/s or more suffice).
+// many subgrids; IDG_CHUNKS_AUTO / IDG_CHUNKS_ADAPTIVE: kAutoChunks chunks
+// whose sizes grow by `ratio` from one to the next (`growing`) or shrink by
+// it (otherwise), chunks under kMinChunk subgrids merged into their
+// neighbour; anything else: one chunk.  A growing chunk's copy keeps ahead of
+// the previous chunk's kernels while the copy rate is at least `ratio` times
+// the rate the kernels consume visibilities (about 61 GB/s for the config-2
+// gridder: at ratio 1.6, copies at 98 GB/s or more suffice).
 constexpr int64_t kMinChunk = 1024;
 constexpr int kAutoChunks = 10;
 constexpr double kAutoRatio = 1.6;
-std::vector<int64_t> chunk_bounds(int64_t n, int64_t chunk, bool growing) {
+constexpr double kMinRatio = 1.1;
+std::vector<int64_t> chunk_bounds(int64_t n, int64_t chunk, bool growing, double ratio) {
     std::vector<int64_t> b{0};
-    if (chunk == IDG_CHUNKS_AUTO) {
+    if (chunk == IDG_CHUNKS_AUTO || chunk == IDG_CHUNKS_ADAPTIVE) {
         const int k = kAutoChunks;
         double total = 0;
-        for (int i = 0; i < k; ++i) total += std::pow(kAutoRatio, i);
+        for (int i = 0; i < k; ++i) total += std::pow(ratio, i);
         double acc = 0;
         for (int i = 0; i < k; ++i) {
-            acc += std::pow(kAutoRatio, growing ? i : k - 1 - i);
+            acc += std::pow(ratio, growing ? i : k - 1 - i);
             const int64_t e = i == k - 1 ? n : (int64_t)(n * acc / total + 0.5);
             if (e - b.back() >= kMinChunk) b.push_back(e);
         }
@@ -207,15 +209,18 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         }
         if (covered < nr_rows) gaps.push_back({covered, nr_rows});
     }
+    std::lock_guard<std::mutex> lock(g_cycle_mutex);
+    CycleBuffers &B = g_cycle;
+    // the gridding phase's growth ratio (the degridding phase's copies out
+    // have run at the full device-to-host rate on every host measured: it
+    // keeps kAutoRatio)
+    const double ratio = chunk_subgrids == IDG_CHUNKS_ADAPTIVE ? B.next_ratio : kAutoRatio;
     std::vector<Chunk> gch, dch;
-    if (!make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, true), row0, row1, &gch) ||
-        !make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, false), row0, row1, &dch)) {
+    if (!make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, true, ratio), row0, row1, &gch) ||
+        !make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, false, kAutoRatio), row0, row1, &dch)) {
         gch.assign(1, Chunk{0, nr_subgrids, 0, nr_rows});
         dch = gch;
     }
-
-    std::lock_guard<std::mutex> lock(g_cycle_mutex);
-    CycleBuffers &B = g_cycle;
     int dev = 0;
     IDG_CUDA(cudaGetDevice(&dev));
     if (B.device != dev) {
@@ -267,8 +272,14 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     if (int rc = new_event(&h2d_v0, true)) return rc;
     if (int rc = new_event(&h2d_v1, true)) return rc;
     std::vector<cudaEvent_t> h2d_done(gch.size()), deg_done(dch.size()), d2h_b(dch.size()), d2h_e(dch.size());
-    for (size_t i = 0; i < gch.size(); ++i)
+    // around each gridding chunk's kernels on the compute stream: g_go after
+    // the wait for its copy, g_end after its adder
+    std::vector<cudaEvent_t> g_go(gch.size()), g_end(gch.size());
+    for (size_t i = 0; i < gch.size(); ++i) {
         if (int rc = new_event(&h2d_done[i], false)) return rc;
+        if (int rc = new_event(&g_go[i], true)) return rc;
+        if (int rc = new_event(&g_end[i], true)) return rc;
+    }
     for (size_t i = 0; i < dch.size(); ++i) {
         if (int rc = new_event(&deg_done[i], false)) return rc;
         if (int rc = new_event(&d2h_b[i], true)) return rc;
@@ -328,6 +339,7 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     const idg_metadata *d_md = static_cast<const idg_metadata *>(B.md);
     for (size_t i = 0; i < gch.size(); ++i) {
         IDG_CUDA(cudaStreamWaitEvent(B.s_compute, h2d_done[i], 0));
+        IDG_CUDA(cudaEventRecord(g_go[i], B.s_compute));
         const int64_t s0 = gch[i].s0, n = gch[i].s1 - s0;
         if (int rc = idg_grid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,
                                            (const float *)B.k, B.vis_in, (const float *)B.taper, B.aterms,
@@ -335,6 +347,7 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
                                            B.s_compute))
             return rc;
         launches += 3;
+        IDG_CUDA(cudaEventRecord(g_end[i], B.s_compute));
     }
     IDG_CUDA(cudaEventRecord(t_grid1, B.s_compute));
 
@@ -377,19 +390,36 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         IDG_CUDA(cudaMemset(w.status, 0, sizeof(unsigned)));
         return fail(IDG_ERR_DEVICE_CHECK, "a kernel rejected plan entries (status 0x%x)", status);
     }
+    float total = 0, g = 0, d = 0, hv = 0;
+    IDG_CUDA(cudaEventElapsedTime(&total, t_start, t_end));
+    IDG_CUDA(cudaEventElapsedTime(&g, t_grid0, t_grid1));
+    IDG_CUDA(cudaEventElapsedTime(&d, t_grid1, t_deg1));
+    IDG_CUDA(cudaEventElapsedTime(&hv, h2d_v0, h2d_v1));
+    // the gridding kernels' waits for their copies: before the first chunk
+    // (after the grid was zeroed) and between one chunk's end and the next's start
+    double wait = 0;
+    for (size_t i = 0; i < gch.size(); ++i) {
+        float x = 0;
+        IDG_CUDA(cudaEventElapsedTime(&x, i == 0 ? t_grid0 : g_end[i - 1], g_go[i]));
+        wait += x;
+    }
+    if (chunk_subgrids == IDG_CHUNKS_ADAPTIVE && gch.size() > 1 && hv > 0 && g - wait > 0) {
+        // next cycle: at most 0.9 x (copy rate / kernel rate), the largest
+        // ratio whose growing copies still end before their kernels are due
+        // at the average copy rate; copies arrive unevenly, so a cycle whose
+        // kernels waited more than 2 % of the phase also steps the ratio down
+        // by 15 %, and one that did not lets it grow back by 5 %
+        const double by_rate = 0.9 * (g - wait) / hv;
+        const double by_wait = ratio * (wait > 0.02 * g ? 0.85 : 1.05);
+        B.next_ratio = std::min(kAutoRatio, std::max(kMinRatio, std::min(by_rate, by_wait)));
+    }
     if (timing) {
-        float total = 0, g = 0, d = 0;
-        IDG_CUDA(cudaEventElapsedTime(&total, t_start, t_end));
-        IDG_CUDA(cudaEventElapsedTime(&g, t_grid0, t_grid1));
-        IDG_CUDA(cudaEventElapsedTime(&d, t_grid1, t_deg1));
         timing->total_ms = total;
         timing->gridding_ms = g;
         timing->degridding_ms = d;
         timing->h2d_bytes = h2d;
         timing->d2h_bytes = d2h;
         timing->kernel_launches = launches;
-        float hv = 0;
-        IDG_CUDA(cudaEventElapsedTime(&hv, h2d_v0, h2d_v1));
         double dv = 0;
         for (size_t i = 0; i < dch.size(); ++i) {
             float x = 0;
@@ -402,6 +432,8 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         timing->d2h_vis_bytes = d2h_vis;
         timing->grid_chunks = (int64_t)gch.size();
         timing->degrid_chunks = (int64_t)dch.size();
+        timing->gridding_wait_ms = wait;
+        timing->chunk_ratio = (chunk_subgrids == IDG_CHUNKS_AUTO || chunk_subgrids == IDG_CHUNKS_ADAPTIVE) ? ratio : 0.0;
     }
     return IDG_OK;
 }

@@ -103,10 +103,13 @@ class IdgCycleTiming(ctypes.Structure):
         ("d2h_vis_bytes", ctypes.c_int64),
         ("grid_chunks", ctypes.c_int64),
         ("degrid_chunks", ctypes.c_int64),
+        ("gridding_wait_ms", ctypes.c_double),
+        ("chunk_ratio", ctypes.c_double),
     ]
 
 
 CHUNKS_AUTO = -1  # IDG_CHUNKS_AUTO: idg_imaging_cycle sizes its chunks for the copy pipeline
+CHUNKS_ADAPTIVE = -2  # IDG_CHUNKS_ADAPTIVE: ... with the growth ratio learned from the previous cycle
 
 
 class IdgServerConfig(ctypes.Structure):

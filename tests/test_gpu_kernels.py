@@ -496,17 +496,22 @@ def test_host_buffer_cycle_auto_chunks(idg):
     vis_h = vis_d.cpu().numpy()
     out_h = np.zeros_like(vis_h)
     grid_h = np.zeros((1, 4, G, G), np.complex64)
-    t = ops.imaging_cycle(gs, obs.metadata, obs.uvw, obs.wavenumbers, vis_h, obs.taper,
-                          np.ascontiguousarray(obs.aterms), out_h, grid_out=grid_h, chunk_subgrids=L.CHUNKS_AUTO)
-    print(f"[cycle] auto chunks: {t['grid_chunks']} gridding, {t['degrid_chunks']} degridding")
-    assert t["grid_chunks"] > 1 and t["degrid_chunks"] > 1
-    assert t["h2d_bytes"] >= vis_h.nbytes + obs.uvw.nbytes
-    check_rel("host cycle auto chunks grid", grid_h, g_ref.cpu().numpy(), TOL)
-    check_rel("host cycle auto chunks vis", out_h, v_ref.cpu().numpy(), TOL)
+    for mode in (L.CHUNKS_AUTO, L.CHUNKS_ADAPTIVE, L.CHUNKS_ADAPTIVE):
+        out_h[...] = 0
+        grid_h[...] = 0
+        t = ops.imaging_cycle(gs, obs.metadata, obs.uvw, obs.wavenumbers, vis_h, obs.taper,
+                              np.ascontiguousarray(obs.aterms), out_h, grid_out=grid_h, chunk_subgrids=mode)
+        print(f"[cycle] chunks {mode}: {t['grid_chunks']} gridding, {t['degrid_chunks']} degridding, "
+              f"ratio {t['chunk_ratio']:.3f}, gridding waited {t['gridding_wait_ms']:.2f} of {t['gridding_ms']:.2f} ms")
+        assert t["grid_chunks"] > 1 and t["degrid_chunks"] > 1
+        assert 1.1 <= t["chunk_ratio"] <= 1.6 and 0 <= t["gridding_wait_ms"] <= t["gridding_ms"]
+        assert t["h2d_bytes"] >= vis_h.nbytes + obs.uvw.nbytes
+        check_rel(f"host cycle chunks {mode} grid", grid_h, g_ref.cpu().numpy(), TOL)
+        check_rel(f"host cycle chunks {mode} vis", out_h, v_ref.cpu().numpy(), TOL)
     ops.release_buffers()
 
 
-@pytest.mark.parametrize("chunk", [0, 5, -1])
+@pytest.mark.parametrize("chunk", [0, 5, -1, -2])
 @pytest.mark.parametrize("locked", [False, True])
 def test_host_buffer_cycle_matches_device_steps(idg, chunk, locked):
     """idg_imaging_cycle on host buffers (pageable numpy arrays, or page-locked
