@@ -537,15 +537,18 @@ IDG_API int idg_reference_dataset(int64_t grid_size, int64_t subgrid_size, int64
 /* Launch shapes of the batched kernels and their autotuner            */
 /* ------------------------------------------------------------------ */
 /* The batched gridder and degridder are compiled in several launch shapes
- * (threads per CTA, pixel pairs per thread, staging tile, CTAs per SM).  The
- * shape used for a subgrid size on the current device is 0 until set here or
- * by idg_autotune().  No counterpart in the reference. */
+ * (threads per CTA, pixels, quads or octets per thread, staging tile, CTAs
+ * per SM).  Until set here or by idg_autotune(), a subgrid size uses the
+ * shapes measured fastest for it on GB300 (the mirror-quad kernels where
+ * their layout fits the size).  No counterpart in the reference. */
 IDG_API int idg_batched_shapes(int *gridder_shapes, int *degridder_shapes);
 IDG_API int idg_set_batched_shapes(int subgrid_size, int gridder_shape, int degridder_shape);
 IDG_API int idg_get_batched_shapes(int subgrid_size, int *gridder_shape, int *degridder_shape);
 /* Times every shape of both batched kernels on the given (device) plan and
  * data -- writes `subgrids` and `visibilities_out` -- and selects the fastest
- * for params->subgrid_size on the current device.  gridder_ms / degridder_ms
+ * for params->subgrid_size on the current device; the shape in use before
+ * keeps its place unless another is more than 1 % faster (sample timings of
+ * shapes that close change from run to run).  gridder_ms / degridder_ms
  * receive the mean time of each shape (arrays of the sizes idg_batched_shapes
  * reports).  Synchronises `stream`. */
 IDG_API int idg_autotune(const idg_params *params, int64_t nr_subgrids, const idg_metadata *metadata,

@@ -11,11 +11,13 @@
 // The pixel centres sit half a cell off the DFT lattice (l = (x+1/2-S/2)/S * image_size),
 // which is where the e^{i pi j/S} factors come from.
 //
-// Kernel: a CTA transforms PLANES (subgrid, polarisation) planes.  Planes are
-// loaded with coalesced 16-byte accesses, eight in flight per thread, into
-// padded shared memory; one thread per row runs a register-resident radix-2
-// (x radix-3 for S = 24, 48) FFT, then one thread per column does the same,
-// and the planes are stored back with 16-byte stores.
+// Kernel: a CTA transforms PLANES (subgrid, polarisation) planes.  One
+// thread per row loads its row straight into registers (16-byte loads; the
+// rows of a CTA stay in L1 while a warp's loads walk them), pre-multiplies
+// it and runs a register-resident radix-2 (x radix-3 for S = 24, 48) FFT; the
+// rows pass through padded shared memory once, as a transpose; one thread per
+// column then transforms its column and stores it post-multiplied, a warp
+// writing whole rows.
 //
 // Split + backward FFT (SPLIT): the degridding step's splitter and backward
 // FFT in one pass.  The load stage reads each plane's footprint on the uv-grid
@@ -141,12 +143,12 @@ template <int S, int DIR, bool SPLIT>
 __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float2 *data, int64_t nr_planes,
                                                                           const float *taper, SplitArgs sa) {
     static_assert(!SPLIT || DIR < 0, "the split pass runs before the backward transform");
+    static_assert(S % 2 == 0, "rows are read as pairs of pixels");
     using Sh = FftShape<S>;
     __shared__ float2 tw[S];      // e^{+2 pi i m / S}
     __shared__ float2 post[S];    // c_j = (-1)^j e^{+i pi (j - S/2)/S}
     __shared__ float2 buf[Sh::planes][S][Sh::pitch];
     __shared__ PlaneSrc src_of[SPLIT ? Sh::planes : 1];
-    constexpr int kBatch = 8;     // 16-byte loads in flight per thread
 
     const int tid = threadIdx.x;
     if (tid < S) {
@@ -177,68 +179,68 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
     }
     __syncthreads();
 
-    // load + pre-multiply: two complex values per 16-byte load, a batch of
-    // independent loads in flight per thread before any of them is used
-    const int total2 = nplanes * S * S / 2;  // float4 elements of this CTA's planes
-    const float4 *src = reinterpret_cast<const float4 *>(data + plane0 * S * S);
-    for (int base = 0; base < total2; base += kBatch * Sh::threads) {
-        float4 v[kBatch];
-#pragma unroll
-        for (int k = 0; k < kBatch; ++k) {
-            const int e2 = base + tid + k * Sh::threads;
-            if (!SPLIT) {
-                v[k] = e2 < total2 ? src[e2] : make_float4(0.f, 0.f, 0.f, 0.f);
-            } else {
-                // two neighbouring pixels of one plane's row, each read from the grid
-                v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (e2 < total2) {
-                    const int e = 2 * e2, pl = e / (S * S), q = e - pl * S * S, y = q / S, x = q - y * S;
-                    const PlaneSrc ps = src_of[pl];
-                    const int step = ps.mirror ? -1 : 1;
-                    const int gy = ps.y0 + step * y, gx = ps.x0 + step * x;
-                    if (ps.base >= 0 && gy >= 0 && gy < sa.G) {
-                        const float2 *row = sa.grid + ps.base + (int64_t)gy * sa.G;
-                        float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-                        if (gx >= 0 && gx < sa.G) a = __ldg(row + gx);
-                        if (gx + step >= 0 && gx + step < sa.G) b = __ldg(row + gx + step);
-                        if (ps.mirror) {
-                            a.y = -a.y;
-                            b.y = -b.y;
-                        }
-                        v[k] = make_float4(a.x, a.y, b.x, b.y);
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kBatch; ++k) {
-            const int e2 = base + tid + k * Sh::threads;
-            if (e2 >= total2) continue;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int e = 2 * e2 + h;
-                const int pl = e / (S * S), q = e - pl * S * S, y = q / S, x = q - y * S;
-                float2 w = h ? make_float2(v[k].z, v[k].w) : make_float2(v[k].x, v[k].y);
-                if (DIR > 0) {
-                    const float f = (((x + y) & 1) ? -1.f : 1.f) * (taper ? __ldg(taper + q) : 1.f);
-                    w = make_float2(w.x * f, w.y * f);
-                } else {
-                    const float2 cy = post[y], cx = post[x];
-                    const cf c = cconj(cmul({cy.x, cy.y}, {cx.x, cx.y}));
-                    const cf r = cmul({w.x, w.y}, c);
-                    w = make_float2(r.re, r.im);
-                }
-                buf[pl][y][x] = w;
-            }
-        }
-    }
-    __syncthreads();
-
     const int pl = tid / S, r = tid - (tid / S) * S;
     cf x[S];
-    if (pl < nplanes) {
+    if (!SPLIT) {
+        // Contiguous planes: coalesced 16-byte loads, eight in flight per
+        // thread, pre-multiplied into padded shared memory; thread (pl, r)
+        // then takes row r of plane pl from there.
+        constexpr int kBatch = 8;
+        const int total2 = nplanes * S * S / 2;  // float4 elements of this CTA's planes
+        const float4 *src = reinterpret_cast<const float4 *>(data + plane0 * S * S);
+        for (int base = 0; base < total2; base += kBatch * Sh::threads) {
+            float4 v[kBatch];
 #pragma unroll
-        for (int i = 0; i < S; ++i) x[i] = {buf[pl][r][i].x, buf[pl][r][i].y};
+            for (int k = 0; k < kBatch; ++k) {
+                const int e2 = base + tid + k * Sh::threads;
+                v[k] = e2 < total2 ? src[e2] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                const int e2 = base + tid + k * Sh::threads;
+                if (e2 >= total2) continue;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int e = 2 * e2 + h;
+                    const int p2 = e / (S * S), q = e - p2 * S * S, y = q / S, xx = q - y * S;
+                    float2 w = h ? make_float2(v[k].z, v[k].w) : make_float2(v[k].x, v[k].y);
+                    if (DIR > 0) {
+                        const float f = (((xx + y) & 1) ? -1.f : 1.f) * (taper ? __ldg(taper + q) : 1.f);
+                        w = make_float2(w.x * f, w.y * f);
+                    } else {
+                        const float2 cy = post[y], cx = post[xx];
+                        const cf c = cconj(cmul({cy.x, cy.y}, {cx.x, cx.y}));
+                        const cf rr = cmul({w.x, w.y}, c);
+                        w = make_float2(rr.re, rr.im);
+                    }
+                    buf[p2][y][xx] = w;
+                }
+            }
+        }
+        __syncthreads();
+        if (pl < nplanes) {
+#pragma unroll
+            for (int i = 0; i < S; ++i) x[i] = {buf[pl][r][i].x, buf[pl][r][i].y};
+        }
+    } else if (pl < nplanes) {
+        // The split pass gathers grid rows: thread (pl, r) reads row r of its
+        // plane's footprint straight into registers and pre-multiplies it.
+        const PlaneSrc ps = src_of[pl];
+        const int step = ps.mirror ? -1 : 1;
+        const int gy = ps.y0 + step * r;
+        const bool row_ok = ps.base >= 0 && gy >= 0 && gy < sa.G;
+        const float2 *grow = sa.grid + (row_ok ? ps.base + (int64_t)gy * sa.G : 0);
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+            const int gx = ps.x0 + step * i;
+            float2 v = make_float2(0.f, 0.f);
+            if (row_ok && gx >= 0 && gx < sa.G) v = __ldg(grow + gx);
+            const float2 cy = post[r], cx = post[i];
+            const cf c = cconj(cmul({cy.x, cy.y}, {cx.x, cx.y}));
+            x[i] = cmul({v.x, ps.mirror ? -v.y : v.y}, c);
+        }
+    }
+    if (pl < nplanes) {
         fft_1d<S, DIR>(x, tw);
 #pragma unroll
         for (int i = 0; i < S; ++i) buf[pl][r][i] = make_float2(x[i].re, x[i].im);
@@ -248,31 +250,21 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
 #pragma unroll
         for (int i = 0; i < S; ++i) x[i] = {buf[pl][i][r].x, buf[pl][i][r].y};
         fft_1d<S, DIR>(x, tw);
+        float2 *dst = data + (plane0 + pl) * S * S;
 #pragma unroll
-        for (int i = 0; i < S; ++i) buf[pl][i][r] = make_float2(x[i].re, x[i].im);
-    }
-    __syncthreads();
-
-    // post-multiply + store, two complex values per 16-byte store
-    float4 *dst = reinterpret_cast<float4 *>(data + plane0 * S * S);
-    for (int e2 = tid; e2 < total2; e2 += Sh::threads) {
-        float2 o[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int e = 2 * e2 + h;
-            const int pl2 = e / (S * S), q = e - pl2 * S * S, y = q / S, xx = q - y * S;
-            float2 v = buf[pl2][y][xx];
+        for (int i = 0; i < S; ++i) {
+            // element (y = i, x = r)
+            float2 v = make_float2(x[i].re, x[i].im);
             if (DIR > 0) {
-                const float2 cy = post[y], cx = post[xx];
+                const float2 cy = post[i], cx = post[r];
                 const cf r2 = cmul(cmul({v.x, v.y}, {cy.x, cy.y}), {cx.x, cx.y});
                 v = make_float2(r2.re, r2.im);
             } else {
-                const float f = (((xx + y) & 1) ? -1.f : 1.f) * (taper ? __ldg(taper + q) : 1.f);
+                const float f = (((r + i) & 1) ? -1.f : 1.f) * (taper ? __ldg(taper + i * S + r) : 1.f);
                 v = make_float2(v.x * f, v.y * f);
             }
-            o[h] = v;
+            dst[i * S + r] = v;
         }
-        dst[e2] = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
     }
 }
 

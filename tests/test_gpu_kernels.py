@@ -361,7 +361,9 @@ def test_every_batched_shape_and_the_autotuner(oracle_mod, idg):
                           store=False)
     assert len(res["gridder_ms"]) == ng and all(t > 0 for t in res["gridder_ms"])
     assert tuning.get_shapes(S) == (res["gridder"], res["degridder"])
-    assert res["gridder_ms"][res["gridder"]] == min(res["gridder_ms"])
+    # the fastest shape, or the one in use before when within 1 % of it
+    assert res["gridder_ms"][res["gridder"]] <= 1.01 * min(res["gridder_ms"]) + 1e-9
+    assert res["degridder_ms"][res["degridder"]] <= 1.01 * min(res["degridder_ms"]) + 1e-9
     tuning.set_shapes(S, *saved)
 
 
