@@ -230,14 +230,20 @@ __global__ void __launch_bounds__(FftShape<S>::threads) subgrid_fft_kernel(float
         const int gy = ps.y0 + step * r;
         const bool row_ok = ps.base >= 0 && gy >= 0 && gy < sa.G;
         const float2 *grow = sa.grid + (row_ok ? ps.base + (int64_t)gy * sa.G : 0);
+        // all of the row's loads first (independent, in flight together),
+        // then the pre-multiplication
 #pragma unroll
         for (int i = 0; i < S; ++i) {
             const int gx = ps.x0 + step * i;
             float2 v = make_float2(0.f, 0.f);
             if (row_ok && gx >= 0 && gx < sa.G) v = __ldg(grow + gx);
+            x[i] = {v.x, ps.mirror ? -v.y : v.y};
+        }
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
             const float2 cy = post[r], cx = post[i];
             const cf c = cconj(cmul({cy.x, cy.y}, {cx.x, cx.y}));
-            x[i] = cmul({v.x, ps.mirror ? -v.y : v.y}, c);
+            x[i] = cmul(x[i], c);
         }
     }
     if (pl < nplanes) {
