@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define IDG_ABI_VERSION 3
+#define IDG_ABI_VERSION 4
 
 typedef enum idg_status {
     IDG_OK = 0,
@@ -441,6 +441,9 @@ typedef struct idg_cycle_timing {
      * (within gridding_ms), and the growth ratio of the chunks. */
     double gridding_wait_ms;
     double chunk_ratio;
+    /* From the call's first copy in to the end of this cycle's copies out
+     * (idg_imaging_cycles; for idg_imaging_cycle it equals total_ms). */
+    double end_ms;
 } idg_cycle_timing;
 
 /* chunk_subgrids of idg_imaging_cycle: chunks sized for the copy pipeline */
@@ -476,6 +479,37 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
                               const float *wavenumbers, const void *visibilities_in, const float *spheroidal,
                               const void *aterms, void *visibilities_out, void *grid_out, int64_t chunk_subgrids,
                               idg_cycle_timing *timing);
+
+/* One cycle of idg_imaging_cycles: its plan, uvw rows and visibilities on
+ * host buffers, as idg_imaging_cycle takes them. */
+typedef struct idg_cycle_io {
+    int64_t nr_subgrids;
+    const idg_metadata *metadata;
+    int64_t nr_rows;
+    const float *uvw;
+    const void *visibilities_in;
+    void *visibilities_out;
+    void *grid_out;           /* may be NULL */
+    idg_cycle_timing *timing; /* may be NULL */
+} idg_cycle_io;
+
+/* A run of imaging cycles on host buffers that share the wavenumbers, taper
+ * and A-terms (copied in once), each cycle as idg_imaging_cycle runs it, with
+ * the same outputs.  Cycle i+1's copies in (plan, uvw, visibilities) start as
+ * soon as cycle i's gridding has read its visibilities, and so run while
+ * cycle i degrids: after the first cycle, the gridding kernels find their
+ * visibilities on the device when the host copy rate is at least the
+ * visibilities in / (degridding + gridding time).  Because cycle i+1 reads
+ * its host inputs before cycle i has written its outputs, no cycle may read
+ * host memory that an earlier cycle of the call writes (IDG_ERR_INVALID_ARGUMENT;
+ * to feed one cycle's output to the next, call idg_imaging_cycle per cycle).
+ * Cycles may share their input and output buffers.  Each cycle's timing
+ * reports its own copies and phases; total_ms runs from its own first copy
+ * in, end_ms from the call's.  With IDG_CHUNKS_ADAPTIVE the first cycle sets
+ * the ratio for the next call.  At most 65536 cycles per call. */
+IDG_API int idg_imaging_cycles(const idg_params *params, int variant, int64_t nr_cycles, const idg_cycle_io *cycles,
+                               const float *wavenumbers, const float *spheroidal, const void *aterms,
+                               int64_t chunk_subgrids);
 IDG_API int idg_release_buffers(void);
 
 /* ------------------------------------------------------------------ */

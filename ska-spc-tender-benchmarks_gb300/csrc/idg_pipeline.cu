@@ -1,5 +1,5 @@
 // idg_pipeline.cu -- the gridding and degridding steps, and the host-buffer
-// imaging cycle with copy/compute overlap.
+// imaging cycles with copy/compute overlap.
 //
 // Gridding step   : gridder (taper off) -> subgrid FFT +1 (taper fused) -> adder
 // Degridding step : splitter -> subgrid FFT -1 (taper fused) -> degridder (taper off)
@@ -7,6 +7,7 @@
 // FFT's pre/post multiplication, where it costs nothing extra.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -31,15 +32,17 @@ struct CycleBuffers {
     int device = -1;
     void *uvw = nullptr, *k = nullptr, *taper = nullptr, *aterms = nullptr, *md = nullptr;
     void *vis_in = nullptr, *vis_out = nullptr, *subgrids = nullptr, *grid = nullptr;
+    void *uvw2 = nullptr, *md2 = nullptr; // the odd cycles' plan and uvw in a call of several cycles
     size_t b_uvw = 0, b_k = 0, b_taper = 0, b_aterms = 0, b_md = 0, b_vis = 0, b_vis_out = 0, b_sub = 0, b_grid = 0;
+    size_t b_uvw2 = 0, b_md2 = 0;
     cudaStream_t s_compute = nullptr, s_h2d = nullptr, s_d2h = nullptr;
-    double next_ratio = 1.6; // IDG_CHUNKS_ADAPTIVE: the ratio the next cycle uses
+    double next_ratio = 1.6; // IDG_CHUNKS_ADAPTIVE: the ratio the next call uses
 
     void release() {
-        for (void *p : {uvw, k, taper, aterms, md, vis_in, vis_out, subgrids, grid})
+        for (void *p : {uvw, k, taper, aterms, md, vis_in, vis_out, subgrids, grid, uvw2, md2})
             if (p) cudaFree(p);
-        uvw = k = taper = aterms = md = vis_in = vis_out = subgrids = grid = nullptr;
-        b_uvw = b_k = b_taper = b_aterms = b_md = b_vis = b_vis_out = b_sub = b_grid = 0;
+        uvw = k = taper = aterms = md = vis_in = vis_out = subgrids = grid = uvw2 = md2 = nullptr;
+        b_uvw = b_k = b_taper = b_aterms = b_md = b_vis = b_vis_out = b_sub = b_grid = b_uvw2 = b_md2 = 0;
         for (cudaStream_t s : {s_compute, s_h2d, s_d2h})
             if (s) cudaStreamDestroy(s);
         s_compute = s_h2d = s_d2h = nullptr;
@@ -170,56 +173,128 @@ IDG_API int idg_release_buffers(void) {
     return IDG_OK;
 }
 
-IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_subgrids,
-                              const idg_metadata *metadata, int64_t nr_rows, const float *uvw,
-                              const float *wavenumbers, const void *visibilities_in, const float *spheroidal,
-                              const void *aterms, void *visibilities_out, void *grid_out, int64_t chunk_subgrids,
-                              idg_cycle_timing *timing) {
+} // extern "C"
+
+namespace {
+
+// One cycle of a host-buffer call: the rows its entries name, its chunks, the
+// device buffers of its plan and uvw, and the events that order it against
+// the cycles either side and time it.
+struct CycleRun {
+    const idg_cycle_io *io = nullptr;
+    std::vector<std::pair<int64_t, int64_t>> gaps; // rows no entry names
+    std::vector<Chunk> gch, dch;
+    void *md = nullptr, *uvw = nullptr;
+    cudaEvent_t t_start, md_in, t_grid0, t_grid1, t_deg1, t_end, h2d_v0, h2d_v1;
+    // per gridding chunk: its copies done (h2d_done), its kernels started
+    // after the wait for them (g_go) and ended with its adder (g_end); per
+    // degridding chunk: its kernels done, its copy out bracketed on s_d2h
+    std::vector<cudaEvent_t> h2d_done, g_go, g_end, deg_done, d2h_b, d2h_e;
+    int64_t launches = 0, h2d = 0, d2h = 0, h2d_vis = 0, d2h_vis = 0;
+};
+
+constexpr int kMaxCycles = 1 << 16; // cycles of one idg_imaging_cycles call
+
+bool ranges_overlap(const void *a, size_t na, const void *b, size_t nb) {
+    if (!a || !b || na == 0 || nb == 0) return false;
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return x < y + nb && y < x + na;
+}
+
+// The cycles of idg_imaging_cycle (one) and idg_imaging_cycles (several),
+// enqueued on the three streams of the cycle buffers.  Cycle i+1's copies in
+// wait only for cycle i's gridding (the last reader of the visibilities in;
+// its plan and uvw go to the other one of two buffers), so they run while
+// cycle i degrids.  Cycle i+1's degridding waits for cycle i's copies out (the
+// visibilities out are one buffer), and its gridding for cycle i's grid copy
+// when there is one.
+int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const idg_cycle_io *io,
+               const float *wavenumbers, const float *spheroidal, const void *aterms, int64_t chunk_subgrids,
+               bool single) {
     if (int rc = check_params(params, true)) return rc;
-    if (nr_subgrids < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_subgrids < 1");
-    if (nr_rows < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "nr_rows < 1");
-    if (!metadata || !uvw || !wavenumbers || !visibilities_in || !spheroidal || !aterms || !visibilities_out)
-        return fail(IDG_ERR_INVALID_ARGUMENT, "NULL host array");
+    if (!single && (nr_cycles < 1 || nr_cycles > kMaxCycles || !io))
+        return fail(IDG_ERR_INVALID_ARGUMENT, "nr_cycles outside [1, %d] or NULL cycles", kMaxCycles);
     const int64_t S = params->subgrid_size, C = params->nr_channels, G = params->grid_size;
     const int64_t W = params->nr_w_planes > 0 ? params->nr_w_planes : 1;
+    const size_t row_bytes = (size_t)C * 32, b_grid = (size_t)W * 4 * G * G * 8;
 
-    // rows of every entry, checked; then the chunks of each phase (rows must
-    // advance chunk by chunk for the copies to overlap the kernels)
-    const int bo1 = metadata[0].baseline_offset;
-    std::vector<int64_t> row0(nr_subgrids), row1(nr_subgrids);
-    for (int64_t s = 0; s < nr_subgrids; ++s) {
-        const idg_metadata &m = metadata[s];
-        const int64_t a = (int64_t)(m.baseline_offset - bo1) + m.time_offset;
-        if (a < 0 || m.nr_timesteps < 0 || a + m.nr_timesteps > nr_rows)
-            return fail(IDG_ERR_INVALID_ARGUMENT, "plan entry %lld names rows outside [0, %lld)", (long long)s,
-                        (long long)nr_rows);
-        row0[s] = a;
-        row1[s] = a + m.nr_timesteps;
-    }
-    // rows that no entry names (zeroed in the output instead of degridded)
-    std::vector<std::pair<int64_t, int64_t>> gaps;
-    {
-        std::vector<std::pair<int64_t, int64_t>> spans(nr_subgrids);
-        for (int64_t s = 0; s < nr_subgrids; ++s) spans[s] = {row0[s], row1[s]};
+    std::vector<CycleRun> runs(nr_cycles);
+    std::vector<std::vector<int64_t>> row0(nr_cycles), row1(nr_cycles);
+    int64_t max_sub = 0, max_rows = 0;
+    for (int64_t i = 0; i < nr_cycles; ++i) {
+        const idg_cycle_io &c = io[i];
+        char tag[40] = "";
+        if (!single) std::snprintf(tag, sizeof tag, "cycle %lld: ", (long long)i);
+        if (c.nr_subgrids < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "%snr_subgrids < 1", tag);
+        if (c.nr_rows < 1) return fail(IDG_ERR_INVALID_ARGUMENT, "%snr_rows < 1", tag);
+        if (!c.metadata || !c.uvw || !wavenumbers || !c.visibilities_in || !spheroidal || !aterms ||
+            !c.visibilities_out)
+            return fail(IDG_ERR_INVALID_ARGUMENT, "%sNULL host array", tag);
+        // rows of every entry, checked; the chunks of each phase follow under
+        // the lock (rows must advance chunk by chunk for the copies to
+        // overlap the kernels)
+        CycleRun &r = runs[i];
+        r.io = &c;
+        const int bo1 = c.metadata[0].baseline_offset;
+        std::vector<int64_t> &a0 = row0[i], &a1 = row1[i];
+        a0.resize(c.nr_subgrids);
+        a1.resize(c.nr_subgrids);
+        for (int64_t s = 0; s < c.nr_subgrids; ++s) {
+            const idg_metadata &m = c.metadata[s];
+            const int64_t a = (int64_t)(m.baseline_offset - bo1) + m.time_offset;
+            if (a < 0 || m.nr_timesteps < 0 || a + m.nr_timesteps > c.nr_rows)
+                return fail(IDG_ERR_INVALID_ARGUMENT, "%splan entry %lld names rows outside [0, %lld)", tag,
+                            (long long)s, (long long)c.nr_rows);
+            a0[s] = a;
+            a1[s] = a + m.nr_timesteps;
+        }
+        // rows that no entry names (zeroed in the output instead of degridded)
+        std::vector<std::pair<int64_t, int64_t>> spans(c.nr_subgrids);
+        for (int64_t s = 0; s < c.nr_subgrids; ++s) spans[s] = {a0[s], a1[s]};
         std::sort(spans.begin(), spans.end());
         int64_t covered = 0;
         for (const auto &sp : spans) {
-            if (sp.first > covered) gaps.push_back({covered, sp.first});
+            if (sp.first > covered) r.gaps.push_back({covered, sp.first});
             covered = std::max(covered, sp.second);
         }
-        if (covered < nr_rows) gaps.push_back({covered, nr_rows});
+        if (covered < c.nr_rows) r.gaps.push_back({covered, c.nr_rows});
+        max_sub = std::max(max_sub, c.nr_subgrids);
+        max_rows = std::max(max_rows, c.nr_rows);
     }
+    // A cycle's copies in start before the cycles ahead of it have copied
+    // their results out: no cycle may read host memory an earlier one writes.
+    for (int64_t i = 0; i < nr_cycles; ++i)
+        for (int64_t j = i + 1; j < nr_cycles; ++j) {
+            const idg_cycle_io &a = io[i], &b = io[j];
+            const size_t out = (size_t)a.nr_rows * row_bytes;
+            const void *writes[2] = {a.visibilities_out, a.grid_out};
+            const size_t wn[2] = {out, a.grid_out ? b_grid : 0};
+            const void *reads[3] = {b.visibilities_in, b.uvw, b.metadata};
+            const size_t rn[3] = {(size_t)b.nr_rows * row_bytes, (size_t)b.nr_rows * 12,
+                                  (size_t)b.nr_subgrids * sizeof(idg_metadata)};
+            for (int x = 0; x < 2; ++x)
+                for (int y = 0; y < 3; ++y)
+                    if (ranges_overlap(writes[x], wn[x], reads[y], rn[y]))
+                        return fail(IDG_ERR_INVALID_ARGUMENT,
+                                    "cycle %lld reads host memory that cycle %lld writes: run them as separate "
+                                    "calls",
+                                    (long long)j, (long long)i);
+        }
+
     std::lock_guard<std::mutex> lock(g_cycle_mutex);
     CycleBuffers &B = g_cycle;
     // the gridding phase's growth ratio (the degridding phase's copies out
     // have run at the full device-to-host rate on every host measured: it
     // keeps kAutoRatio)
     const double ratio = chunk_subgrids == IDG_CHUNKS_ADAPTIVE ? B.next_ratio : kAutoRatio;
-    std::vector<Chunk> gch, dch;
-    if (!make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, true, ratio), row0, row1, &gch) ||
-        !make_chunks(chunk_bounds(nr_subgrids, chunk_subgrids, false, kAutoRatio), row0, row1, &dch)) {
-        gch.assign(1, Chunk{0, nr_subgrids, 0, nr_rows});
-        dch = gch;
+    for (int64_t i = 0; i < nr_cycles; ++i) {
+        CycleRun &r = runs[i];
+        const int64_t n = r.io->nr_subgrids;
+        if (!make_chunks(chunk_bounds(n, chunk_subgrids, true, ratio), row0[i], row1[i], &r.gch) ||
+            !make_chunks(chunk_bounds(n, chunk_subgrids, false, kAutoRatio), row0[i], row1[i], &r.dch)) {
+            r.gch.assign(1, Chunk{0, n, 0, r.io->nr_rows});
+            r.dch = r.gch;
+        }
     }
     int dev = 0;
     IDG_CUDA(cudaGetDevice(&dev));
@@ -232,10 +307,10 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         IDG_CUDA(cudaStreamCreateWithFlags(&B.s_h2d, cudaStreamNonBlocking));
         IDG_CUDA(cudaStreamCreateWithFlags(&B.s_d2h, cudaStreamNonBlocking));
     }
-    const size_t b_uvw = (size_t)nr_rows * 12, b_k = (size_t)C * 4, b_taper = (size_t)S * S * 4,
+    const size_t b_uvw = (size_t)max_rows * 12, b_k = (size_t)C * 4, b_taper = (size_t)S * S * 4,
                  b_aterms = (size_t)params->nr_aterms * params->nr_stations * S * S * 32,
-                 b_md = (size_t)nr_subgrids * sizeof(idg_metadata), b_vis = (size_t)nr_rows * C * 32,
-                 b_sub = (size_t)nr_subgrids * 4 * S * S * 8, b_grid = (size_t)W * 4 * G * G * 8;
+                 b_md = (size_t)max_sub * sizeof(idg_metadata), b_vis = (size_t)max_rows * row_bytes,
+                 b_sub = (size_t)max_sub * 4 * S * S * 8;
     if (int rc = ensure(&B.uvw, &B.b_uvw, b_uvw)) return rc;
     if (int rc = ensure(&B.k, &B.b_k, b_k)) return rc;
     if (int rc = ensure(&B.taper, &B.b_taper, b_taper)) return rc;
@@ -245,6 +320,14 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
     if (int rc = ensure(&B.vis_out, &B.b_vis_out, b_vis)) return rc;
     if (int rc = ensure(&B.subgrids, &B.b_sub, b_sub)) return rc;
     if (int rc = ensure(&B.grid, &B.b_grid, b_grid)) return rc;
+    if (nr_cycles > 1) {
+        if (int rc = ensure(&B.uvw2, &B.b_uvw2, b_uvw)) return rc;
+        if (int rc = ensure(&B.md2, &B.b_md2, b_md)) return rc;
+    }
+    for (int64_t i = 0; i < nr_cycles; ++i) {
+        runs[i].md = i % 2 ? B.md2 : B.md;
+        runs[i].uvw = i % 2 ? B.uvw2 : B.uvw;
+    }
 
     std::vector<cudaEvent_t> ev;
     auto new_event = [&](cudaEvent_t *e, bool timing_event) -> int {
@@ -258,39 +341,34 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
             for (cudaEvent_t e : v) cudaEventDestroy(e);
         }
     } guard{ev};
-
-    cudaEvent_t t_start, t_grid0, t_grid1, t_deg1, t_end, consts_in;
-    if (int rc = new_event(&t_start, true)) return rc;
-    if (int rc = new_event(&t_grid0, true)) return rc;
-    if (int rc = new_event(&t_grid1, true)) return rc;
-    if (int rc = new_event(&t_deg1, true)) return rc;
-    if (int rc = new_event(&t_end, true)) return rc;
-    if (int rc = new_event(&consts_in, false)) return rc;
-    // copy timing: the visibility copies in run back to back on s_h2d
-    // (h2d_v0 .. h2d_v1); each copy out is bracketed on s_d2h (d2h_b, d2h_e)
-    cudaEvent_t h2d_v0, h2d_v1;
-    if (int rc = new_event(&h2d_v0, true)) return rc;
-    if (int rc = new_event(&h2d_v1, true)) return rc;
-    std::vector<cudaEvent_t> h2d_done(gch.size()), deg_done(dch.size()), d2h_b(dch.size()), d2h_e(dch.size());
-    // around each gridding chunk's kernels on the compute stream: g_go after
-    // the wait for its copy, g_end after its adder
-    std::vector<cudaEvent_t> g_go(gch.size()), g_end(gch.size());
-    for (size_t i = 0; i < gch.size(); ++i) {
-        if (int rc = new_event(&h2d_done[i], false)) return rc;
-        if (int rc = new_event(&g_go[i], true)) return rc;
-        if (int rc = new_event(&g_end[i], true)) return rc;
-    }
-    for (size_t i = 0; i < dch.size(); ++i) {
-        if (int rc = new_event(&deg_done[i], false)) return rc;
-        if (int rc = new_event(&d2h_b[i], true)) return rc;
-        if (int rc = new_event(&d2h_e[i], true)) return rc;
+    for (CycleRun &r : runs) {
+        for (cudaEvent_t *e : {&r.t_start, &r.t_grid0, &r.t_grid1, &r.t_deg1, &r.t_end, &r.h2d_v0, &r.h2d_v1})
+            if (int rc = new_event(e, true)) return rc;
+        if (int rc = new_event(&r.md_in, false)) return rc;
+        const size_t ng = r.gch.size(), nd = r.dch.size();
+        r.h2d_done.resize(ng);
+        r.g_go.resize(ng);
+        r.g_end.resize(ng);
+        r.deg_done.resize(nd);
+        r.d2h_b.resize(nd);
+        r.d2h_e.resize(nd);
+        for (size_t i = 0; i < ng; ++i) {
+            if (int rc = new_event(&r.h2d_done[i], false)) return rc;
+            if (int rc = new_event(&r.g_go[i], true)) return rc;
+            if (int rc = new_event(&r.g_end[i], true)) return rc;
+        }
+        for (size_t i = 0; i < nd; ++i) {
+            if (int rc = new_event(&r.deg_done[i], false)) return rc;
+            if (int rc = new_event(&r.d2h_b[i], true)) return rc;
+            if (int rc = new_event(&r.d2h_e[i], true)) return rc;
+        }
     }
 
     DeviceWords w;
     if (int rc = device_words(&w)) return rc;
     IDG_CUDA(cudaDeviceSynchronize());
     // From here on every return -- early ones included -- first waits for the
-    // cycle's streams, so that no copy from or into the caller's host buffers
+    // call's streams, so that no copy from or into the caller's host buffers
     // is still queued when the call returns.  (Declared after the event guard,
     // so it runs before the events are destroyed.)
     struct StreamGuard {
@@ -300,88 +378,110 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         }
     } stream_guard{{B.s_h2d, B.s_compute, B.s_d2h}};
     // The check word is library-wide: clear what earlier, unrelated calls left
-    // in it, so that the status read at the end is this cycle's own.
+    // in it, so that the status read at the end is this call's own.
     IDG_CUDA(cudaMemsetAsync(w.status, 0, sizeof(unsigned), B.s_compute));
-    int64_t launches = 0, h2d = 0, d2h = 0, h2d_vis = 0, d2h_vis = 0;
-    IDG_CUDA(cudaEventRecord(t_start, B.s_h2d));
-    // constants first (small), then each chunk's uvw rows and visibilities
-    IDG_CUDA(cudaMemcpyAsync(B.md, metadata, b_md, cudaMemcpyHostToDevice, B.s_h2d));
-    IDG_CUDA(cudaMemcpyAsync(B.k, wavenumbers, b_k, cudaMemcpyHostToDevice, B.s_h2d));
-    IDG_CUDA(cudaMemcpyAsync(B.taper, spheroidal, b_taper, cudaMemcpyHostToDevice, B.s_h2d));
-    IDG_CUDA(cudaMemcpyAsync(B.aterms, aterms, b_aterms, cudaMemcpyHostToDevice, B.s_h2d));
-    h2d += b_md + b_k + b_taper + b_aterms;
-    IDG_CUDA(cudaEventRecord(consts_in, B.s_h2d));
-    IDG_CUDA(cudaEventRecord(h2d_v0, B.s_h2d));
-    for (size_t i = 0; i < gch.size(); ++i) {
-        const Chunk &c = gch[i];
-        // uvw: this chunk's rows, with any rows before them that no chunk names
-        // (and, for the last chunk, the rows after it)
-        const int64_t u0 = i == 0 ? 0 : gch[i - 1].r1, u1 = i + 1 == gch.size() ? nr_rows : c.r1;
-        if (u1 > u0) {
-            IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.uvw) + (size_t)u0 * 12,
-                                     reinterpret_cast<const char *>(uvw) + (size_t)u0 * 12, (size_t)(u1 - u0) * 12,
-                                     cudaMemcpyHostToDevice, B.s_h2d));
-            h2d += (u1 - u0) * 12;
+
+    for (int64_t ci = 0; ci < nr_cycles; ++ci) {
+        CycleRun &r = runs[ci];
+        const CycleRun *prev = ci > 0 ? &runs[ci - 1] : nullptr;
+        const idg_cycle_io &c = *r.io;
+        const int64_t nr_rows = c.nr_rows;
+        // copies in: after the previous cycle's gridding has read the
+        // visibilities in; the constants once, before the first plan
+        if (prev) IDG_CUDA(cudaStreamWaitEvent(B.s_h2d, prev->t_grid1, 0));
+        IDG_CUDA(cudaEventRecord(r.t_start, B.s_h2d));
+        if (!prev) {
+            IDG_CUDA(cudaMemcpyAsync(B.k, wavenumbers, b_k, cudaMemcpyHostToDevice, B.s_h2d));
+            IDG_CUDA(cudaMemcpyAsync(B.taper, spheroidal, b_taper, cudaMemcpyHostToDevice, B.s_h2d));
+            IDG_CUDA(cudaMemcpyAsync(B.aterms, aterms, b_aterms, cudaMemcpyHostToDevice, B.s_h2d));
+            r.h2d += b_k + b_taper + b_aterms;
         }
-        const size_t off = (size_t)c.r0 * C * 32, bytes = (size_t)(c.r1 - c.r0) * C * 32;
-        IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.vis_in) + off, static_cast<const char *>(visibilities_in) + off,
-                                 bytes, cudaMemcpyHostToDevice, B.s_h2d));
-        h2d += bytes;
-        h2d_vis += bytes;
-        IDG_CUDA(cudaEventRecord(h2d_done[i], B.s_h2d));
-    }
-    IDG_CUDA(cudaEventRecord(h2d_v1, B.s_h2d));
+        const size_t md_bytes = (size_t)c.nr_subgrids * sizeof(idg_metadata);
+        IDG_CUDA(cudaMemcpyAsync(r.md, c.metadata, md_bytes, cudaMemcpyHostToDevice, B.s_h2d));
+        r.h2d += md_bytes;
+        IDG_CUDA(cudaEventRecord(r.md_in, B.s_h2d));
+        IDG_CUDA(cudaEventRecord(r.h2d_v0, B.s_h2d));
+        for (size_t i = 0; i < r.gch.size(); ++i) {
+            const Chunk &k = r.gch[i];
+            // uvw: this chunk's rows, with any rows before them that no chunk
+            // names (and, for the last chunk, the rows after it)
+            const int64_t u0 = i == 0 ? 0 : r.gch[i - 1].r1, u1 = i + 1 == r.gch.size() ? nr_rows : k.r1;
+            if (u1 > u0) {
+                IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(r.uvw) + (size_t)u0 * 12,
+                                         reinterpret_cast<const char *>(c.uvw) + (size_t)u0 * 12,
+                                         (size_t)(u1 - u0) * 12, cudaMemcpyHostToDevice, B.s_h2d));
+                r.h2d += (u1 - u0) * 12;
+            }
+            const size_t off = (size_t)k.r0 * row_bytes, bytes = (size_t)(k.r1 - k.r0) * row_bytes;
+            IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.vis_in) + off,
+                                     static_cast<const char *>(c.visibilities_in) + off, bytes,
+                                     cudaMemcpyHostToDevice, B.s_h2d));
+            r.h2d += bytes;
+            r.h2d_vis += bytes;
+            IDG_CUDA(cudaEventRecord(r.h2d_done[i], B.s_h2d));
+        }
+        IDG_CUDA(cudaEventRecord(r.h2d_v1, B.s_h2d));
 
-    // gridding phase
-    IDG_CUDA(cudaStreamWaitEvent(B.s_compute, consts_in, 0));
-    IDG_CUDA(cudaMemsetAsync(B.grid, 0, b_grid, B.s_compute));
-    IDG_CUDA(cudaEventRecord(t_grid0, B.s_compute));
-    const idg_metadata *d_md = static_cast<const idg_metadata *>(B.md);
-    for (size_t i = 0; i < gch.size(); ++i) {
-        IDG_CUDA(cudaStreamWaitEvent(B.s_compute, h2d_done[i], 0));
-        IDG_CUDA(cudaEventRecord(g_go[i], B.s_compute));
-        const int64_t s0 = gch[i].s0, n = gch[i].s1 - s0;
-        if (int rc = idg_grid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,
-                                           (const float *)B.k, B.vis_in, (const float *)B.taper, B.aterms,
-                                           static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
-                                           B.s_compute))
-            return rc;
-        launches += 3;
-        IDG_CUDA(cudaEventRecord(g_end[i], B.s_compute));
-    }
-    IDG_CUDA(cudaEventRecord(t_grid1, B.s_compute));
+        // gridding phase (after the previous cycle's grid copy, if any: the
+        // grid is zeroed here)
+        IDG_CUDA(cudaStreamWaitEvent(B.s_compute, r.md_in, 0));
+        if (prev && prev->io->grid_out) IDG_CUDA(cudaStreamWaitEvent(B.s_compute, prev->t_end, 0));
+        IDG_CUDA(cudaMemsetAsync(B.grid, 0, b_grid, B.s_compute));
+        IDG_CUDA(cudaEventRecord(r.t_grid0, B.s_compute));
+        const idg_metadata *d_md = static_cast<const idg_metadata *>(r.md);
+        for (size_t i = 0; i < r.gch.size(); ++i) {
+            IDG_CUDA(cudaStreamWaitEvent(B.s_compute, r.h2d_done[i], 0));
+            IDG_CUDA(cudaEventRecord(r.g_go[i], B.s_compute));
+            const int64_t s0 = r.gch[i].s0, n = r.gch[i].s1 - s0;
+            if (int rc = idg_grid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows,
+                                               (const float *)r.uvw, (const float *)B.k, B.vis_in,
+                                               (const float *)B.taper, B.aterms,
+                                               static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
+                                               B.s_compute))
+                return rc;
+            r.launches += 3;
+            IDG_CUDA(cudaEventRecord(r.g_end[i], B.s_compute));
+        }
+        IDG_CUDA(cudaEventRecord(r.t_grid1, B.s_compute));
 
-    // degridding phase: the degridder writes every row a plan entry names;
-    // the rows no entry names come back as zeros
-    for (const auto &gap : gaps)
-        IDG_CUDA(cudaMemsetAsync(static_cast<char *>(B.vis_out) + (size_t)gap.first * C * 32, 0,
-                                 (size_t)(gap.second - gap.first) * C * 32, B.s_compute));
-    for (size_t i = 0; i < dch.size(); ++i) {
-        const int64_t s0 = dch[i].s0, n = dch[i].s1 - s0;
-        if (int rc = idg_degrid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows, (const float *)B.uvw,
-                                             (const float *)B.k, B.vis_out, (const float *)B.taper, B.aterms,
-                                             static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
-                                             B.s_compute))
-            return rc;
-        launches += 3;
-        IDG_CUDA(cudaEventRecord(deg_done[i], B.s_compute));
-        IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, deg_done[i], 0));
-        const size_t off = (size_t)dch[i].r0 * C * 32, bytes = (size_t)(dch[i].r1 - dch[i].r0) * C * 32;
-        IDG_CUDA(cudaEventRecord(d2h_b[i], B.s_d2h));
-        IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(visibilities_out) + off, static_cast<char *>(B.vis_out) + off,
-                                 bytes, cudaMemcpyDeviceToHost, B.s_d2h));
-        IDG_CUDA(cudaEventRecord(d2h_e[i], B.s_d2h));
-        d2h += bytes;
-        d2h_vis += bytes;
+        // degridding phase, after the previous cycle's copies out: the
+        // degridder writes every row a plan entry names; the rows no entry
+        // names come back as zeros
+        if (prev) IDG_CUDA(cudaStreamWaitEvent(B.s_compute, prev->t_end, 0));
+        for (const auto &gap : r.gaps)
+            IDG_CUDA(cudaMemsetAsync(static_cast<char *>(B.vis_out) + (size_t)gap.first * row_bytes, 0,
+                                     (size_t)(gap.second - gap.first) * row_bytes, B.s_compute));
+        for (size_t i = 0; i < r.dch.size(); ++i) {
+            const int64_t s0 = r.dch[i].s0, n = r.dch[i].s1 - s0;
+            if (int rc = idg_degrid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows,
+                                                 (const float *)r.uvw, (const float *)B.k, B.vis_out,
+                                                 (const float *)B.taper, B.aterms,
+                                                 static_cast<char *>(B.subgrids) + (size_t)s0 * 4 * S * S * 8, B.grid,
+                                                 B.s_compute))
+                return rc;
+            r.launches += 3;
+            IDG_CUDA(cudaEventRecord(r.deg_done[i], B.s_compute));
+            IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, r.deg_done[i], 0));
+            // this chunk's rows, with the rows before them that no chunk names
+            // (and, for the last chunk, the rows after it): zeroed above
+            const int64_t v0 = i == 0 ? 0 : r.dch[i - 1].r1, v1 = i + 1 == r.dch.size() ? nr_rows : r.dch[i].r1;
+            const size_t off = (size_t)v0 * row_bytes, bytes = (size_t)(v1 - v0) * row_bytes;
+            IDG_CUDA(cudaEventRecord(r.d2h_b[i], B.s_d2h));
+            IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(c.visibilities_out) + off,
+                                     static_cast<char *>(B.vis_out) + off, bytes, cudaMemcpyDeviceToHost, B.s_d2h));
+            IDG_CUDA(cudaEventRecord(r.d2h_e[i], B.s_d2h));
+            r.d2h += bytes;
+            r.d2h_vis += bytes;
+        }
+        IDG_CUDA(cudaEventRecord(r.t_deg1, B.s_compute));
+        if (c.grid_out) {
+            IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, r.t_grid1, 0));
+            IDG_CUDA(cudaMemcpyAsync(c.grid_out, B.grid, b_grid, cudaMemcpyDeviceToHost, B.s_d2h));
+            r.d2h += b_grid;
+        }
+        IDG_CUDA(cudaEventRecord(r.t_end, B.s_d2h));
     }
-    IDG_CUDA(cudaEventRecord(t_deg1, B.s_compute));
-    if (grid_out) {
-        IDG_CUDA(cudaStreamWaitEvent(B.s_d2h, t_grid1, 0));
-        IDG_CUDA(cudaMemcpyAsync(grid_out, B.grid, b_grid, cudaMemcpyDeviceToHost, B.s_d2h));
-        d2h += b_grid;
-    }
-    IDG_CUDA(cudaEventRecord(t_end, B.s_d2h));
-    IDG_CUDA(cudaEventSynchronize(t_end));
+    IDG_CUDA(cudaEventSynchronize(runs.back().t_end));
     IDG_CUDA(cudaStreamSynchronize(B.s_compute));
 
     unsigned status = 0;
@@ -390,52 +490,79 @@ IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_
         IDG_CUDA(cudaMemset(w.status, 0, sizeof(unsigned)));
         return fail(IDG_ERR_DEVICE_CHECK, "a kernel rejected plan entries (status 0x%x)", status);
     }
-    float total = 0, g = 0, d = 0, hv = 0;
-    IDG_CUDA(cudaEventElapsedTime(&total, t_start, t_end));
-    IDG_CUDA(cudaEventElapsedTime(&g, t_grid0, t_grid1));
-    IDG_CUDA(cudaEventElapsedTime(&d, t_grid1, t_deg1));
-    IDG_CUDA(cudaEventElapsedTime(&hv, h2d_v0, h2d_v1));
-    // the gridding kernels' waits for their copies: before the first chunk
-    // (after the grid was zeroed) and between one chunk's end and the next's start
-    double wait = 0;
-    for (size_t i = 0; i < gch.size(); ++i) {
-        float x = 0;
-        IDG_CUDA(cudaEventElapsedTime(&x, i == 0 ? t_grid0 : g_end[i - 1], g_go[i]));
-        wait += x;
-    }
-    if (chunk_subgrids == IDG_CHUNKS_ADAPTIVE && gch.size() > 1 && hv > 0 && g - wait > 0) {
-        // next cycle: at most 0.9 x (copy rate / kernel rate), the largest
-        // ratio whose growing copies still end before their kernels are due
-        // at the average copy rate; copies arrive unevenly, so a cycle whose
-        // kernels waited more than 2 % of the phase also steps the ratio down
-        // by 15 %, and one that did not lets it grow back by 5 %
-        const double by_rate = 0.9 * (g - wait) / hv;
-        const double by_wait = ratio * (wait > 0.02 * g ? 0.85 : 1.05);
-        B.next_ratio = std::min(kAutoRatio, std::max(kMinRatio, std::min(by_rate, by_wait)));
-    }
-    if (timing) {
+    for (int64_t ci = 0; ci < nr_cycles; ++ci) {
+        const CycleRun &r = runs[ci];
+        float total = 0, g = 0, d = 0, hv = 0, end = 0;
+        IDG_CUDA(cudaEventElapsedTime(&total, r.t_start, r.t_end));
+        IDG_CUDA(cudaEventElapsedTime(&end, runs[0].t_start, r.t_end));
+        IDG_CUDA(cudaEventElapsedTime(&g, r.t_grid0, r.t_grid1));
+        IDG_CUDA(cudaEventElapsedTime(&d, r.t_grid1, r.t_deg1));
+        IDG_CUDA(cudaEventElapsedTime(&hv, r.h2d_v0, r.h2d_v1));
+        // the gridding kernels' waits for their copies: before the first chunk
+        // (after the grid was zeroed) and between one chunk's end and the next's start
+        double wait = 0;
+        for (size_t i = 0; i < r.gch.size(); ++i) {
+            float x = 0;
+            IDG_CUDA(cudaEventElapsedTime(&x, i == 0 ? r.t_grid0 : r.g_end[i - 1], r.g_go[i]));
+            wait += x;
+        }
+        if (ci == 0 && chunk_subgrids == IDG_CHUNKS_ADAPTIVE && r.gch.size() > 1 && hv > 0 && g - wait > 0) {
+            // next call: at most 0.9 x (copy rate / kernel rate), the largest
+            // ratio whose growing copies still end before their kernels are
+            // due at the average copy rate; copies arrive unevenly, so a cycle
+            // whose kernels waited more than 2 % of the phase also steps the
+            // ratio down by 15 %, and one that did not lets it grow back by
+            // 5 %.  Only the call's first cycle counts: the copies of the
+            // cycles after it ran ahead, during the degridding before them.
+            const double by_rate = 0.9 * (g - wait) / hv;
+            const double by_wait = ratio * (wait > 0.02 * g ? 0.85 : 1.05);
+            B.next_ratio = std::min(kAutoRatio, std::max(kMinRatio, std::min(by_rate, by_wait)));
+        }
+        idg_cycle_timing *timing = r.io->timing;
+        if (!timing) continue;
         timing->total_ms = total;
         timing->gridding_ms = g;
         timing->degridding_ms = d;
-        timing->h2d_bytes = h2d;
-        timing->d2h_bytes = d2h;
-        timing->kernel_launches = launches;
+        timing->h2d_bytes = r.h2d;
+        timing->d2h_bytes = r.d2h;
+        timing->kernel_launches = r.launches;
         double dv = 0;
-        for (size_t i = 0; i < dch.size(); ++i) {
+        for (size_t i = 0; i < r.dch.size(); ++i) {
             float x = 0;
-            IDG_CUDA(cudaEventElapsedTime(&x, d2h_b[i], d2h_e[i]));
+            IDG_CUDA(cudaEventElapsedTime(&x, r.d2h_b[i], r.d2h_e[i]));
             dv += x;
         }
         timing->h2d_vis_ms = hv;
         timing->d2h_vis_ms = dv;
-        timing->h2d_vis_bytes = h2d_vis;
-        timing->d2h_vis_bytes = d2h_vis;
-        timing->grid_chunks = (int64_t)gch.size();
-        timing->degrid_chunks = (int64_t)dch.size();
+        timing->h2d_vis_bytes = r.h2d_vis;
+        timing->d2h_vis_bytes = r.d2h_vis;
+        timing->grid_chunks = (int64_t)r.gch.size();
+        timing->degrid_chunks = (int64_t)r.dch.size();
         timing->gridding_wait_ms = wait;
-        timing->chunk_ratio = (chunk_subgrids == IDG_CHUNKS_AUTO || chunk_subgrids == IDG_CHUNKS_ADAPTIVE) ? ratio : 0.0;
+        timing->chunk_ratio =
+            (chunk_subgrids == IDG_CHUNKS_AUTO || chunk_subgrids == IDG_CHUNKS_ADAPTIVE) ? ratio : 0.0;
+        timing->end_ms = end;
     }
     return IDG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+IDG_API int idg_imaging_cycle(const idg_params *params, int variant, int64_t nr_subgrids,
+                              const idg_metadata *metadata, int64_t nr_rows, const float *uvw,
+                              const float *wavenumbers, const void *visibilities_in, const float *spheroidal,
+                              const void *aterms, void *visibilities_out, void *grid_out, int64_t chunk_subgrids,
+                              idg_cycle_timing *timing) {
+    const idg_cycle_io io{nr_subgrids, metadata, nr_rows, uvw, visibilities_in, visibilities_out, grid_out, timing};
+    return run_cycles(params, variant, 1, &io, wavenumbers, spheroidal, aterms, chunk_subgrids, true);
+}
+
+IDG_API int idg_imaging_cycles(const idg_params *params, int variant, int64_t nr_cycles, const idg_cycle_io *cycles,
+                               const float *wavenumbers, const float *spheroidal, const void *aterms,
+                               int64_t chunk_subgrids) {
+    return run_cycles(params, variant, nr_cycles, cycles, wavenumbers, spheroidal, aterms, chunk_subgrids, false);
 }
 
 } // extern "C"

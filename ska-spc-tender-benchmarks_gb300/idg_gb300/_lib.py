@@ -105,6 +105,20 @@ class IdgCycleTiming(ctypes.Structure):
         ("degrid_chunks", ctypes.c_int64),
         ("gridding_wait_ms", ctypes.c_double),
         ("chunk_ratio", ctypes.c_double),
+        ("end_ms", ctypes.c_double),
+    ]
+
+
+class IdgCycleIo(ctypes.Structure):
+    _fields_ = [
+        ("nr_subgrids", ctypes.c_int64),
+        ("metadata", ctypes.c_void_p),
+        ("nr_rows", ctypes.c_int64),
+        ("uvw", ctypes.c_void_p),
+        ("visibilities_in", ctypes.c_void_p),
+        ("visibilities_out", ctypes.c_void_p),
+        ("grid_out", ctypes.c_void_p),
+        ("timing", ctypes.POINTER(IdgCycleTiming)),
     ]
 
 
@@ -218,6 +232,7 @@ _SIGNATURES = {
     "idg_degrid_visibilities": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P],
     "idg_imaging_cycle": [ctypes.POINTER(IdgParams), _I32, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64,
                           ctypes.c_void_p],
+    "idg_imaging_cycles": [ctypes.POINTER(IdgParams), _I32, _I64, ctypes.POINTER(IdgCycleIo), _P, _P, _P, _I64],
     "idg_release_buffers": [],
     "idg_plan_subgrids": [ctypes.POINTER(IdgPlannerParams), _P, _P, _P, _I64, _P, _P, ctypes.POINTER(ctypes.c_int64),
                           _P],

@@ -262,6 +262,33 @@ def imaging_cycle(spec: GridSpec, metadata: np.ndarray, uvw: np.ndarray, wavenum
     return {f: getattr(t, f) for f, _ in _lib.IdgCycleTiming._fields_}
 
 
+def imaging_cycles(spec: GridSpec, cycles, wavenumbers: np.ndarray, taper, aterms, variant=VARIANT_BATCHED,
+                   chunk_subgrids=0) -> list[dict]:
+    """Several grid + degrid cycles on HOST buffers through idg_imaging_cycles,
+    each cycle's copies in running while the cycle before it degrids.
+    `cycles`: a sequence of (metadata, uvw, vis_in, vis_out) or (metadata,
+    uvw, vis_in, vis_out, grid_out) tuples.  Returns one timing dict per cycle."""
+    for name, a in (("wavenumbers", wavenumbers), ("taper", taper)):
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]):
+            raise TypeError(f"{name} must be a C-contiguous float32 numpy array")
+    keep, ios, timings = [], (_lib.IdgCycleIo * max(1, len(cycles)))(), []
+    for i, c in enumerate(cycles):
+        metadata, uvw, vis_in, vis_out = c[:4]
+        grid_out = c[4] if len(c) > 4 else None
+        md = np.ascontiguousarray(metadata, dtype=_lib.METADATA_DTYPE)
+        if not (isinstance(uvw, np.ndarray) and uvw.dtype == np.float32 and uvw.flags["C_CONTIGUOUS"]):
+            raise TypeError(f"cycle {i}: uvw must be a C-contiguous float32 numpy array")
+        t = _lib.IdgCycleTiming()
+        keep.append(md)
+        timings.append(t)
+        ios[i] = _lib.IdgCycleIo(md.shape[0], ptr(md), uvw.shape[0], ptr(uvw), ptr(vis_in), ptr(vis_out),
+                                 ptr(grid_out), ctypes.pointer(t))
+    p = spec.to_c()
+    _lib.call("idg_imaging_cycles", ctypes.byref(p), variant, len(cycles), ios, ptr(wavenumbers), ptr(taper),
+              ptr(aterms), int(chunk_subgrids))
+    return [{f: getattr(t, f) for f, _ in _lib.IdgCycleTiming._fields_} for t in timings]
+
+
 def plan_subgrids(uvw, frequencies, baselines, nr_timesteps: int, subgrid_size: int, grid_size: int,
                   image_size: float, max_timesteps: int, aterm_interval: int = 0, margin: int | None = None,
                   capacity: int | None = None, w_step: float = 0.0, nr_w_planes: int = 1, stream=None):

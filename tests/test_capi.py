@@ -44,7 +44,7 @@ def test_library_exports_every_declared_symbol(idg):
     lib = idg.load()
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.idg_abi_version() == 3
+    assert lib.idg_abi_version() == 4
 
 
 def test_library_is_in_tree(idg):
@@ -87,6 +87,52 @@ def test_argument_errors_before_device_work(idg):
     r = _lib.IdgBenchmarkResult()
     assert lib.idg_gridding_launch(ctypes.byref(cfg), None, None, None, None, None, None, None, None, None, ctypes.byref(r)) == _lib.IDG_ERR_INVALID_ARGUMENT
     assert "niterations" in _lib.last_error()
+
+
+def test_imaging_cycles_argument_errors_before_device_work(idg):
+    """idg_imaging_cycles checks its cycles on the host, before any CUDA call:
+    counts, NULL arrays and rows (reported with the cycle's index), and host
+    memory that a later cycle would read before an earlier one writes it."""
+    from idg_gb300 import _lib
+
+    lib = idg.load()
+    p = _lib.IdgParams(1024, 32, 4, 4, 1, 1, 0.1, 0.0, 0, 0)
+    C, rows = 4, 16
+    md = np.zeros(2, _lib.METADATA_DTYPE)
+    md["nr_timesteps"] = 8
+    md["time_offset"] = [0, 8]
+    uvw = np.zeros((rows, 3), np.float32)
+    k = np.zeros(C, np.float32)
+    taper = np.zeros((32, 32), np.float32)
+    at = np.zeros((1, 4, 32, 32, 4), np.complex64)
+    bufs = [np.zeros((rows, C, 4), np.complex64) for _ in range(4)]
+
+    def io(vin, vout, nr_rows=rows, m=md):
+        return _lib.IdgCycleIo(m.shape[0], m.ctypes.data, nr_rows, uvw.ctypes.data, vin.ctypes.data,
+                               vout.ctypes.data, None, None)
+
+    def run(*cycles, n=None):
+        arr = (_lib.IdgCycleIo * max(1, len(cycles)))(*cycles)
+        return lib.idg_imaging_cycles(ctypes.byref(p), 0, len(cycles) if n is None else n, arr, k.ctypes.data,
+                                      taper.ctypes.data, at.ctypes.data, 0)
+
+    assert lib.idg_imaging_cycles(ctypes.byref(p), 0, 1, None, None, None, None, 0) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert run(io(bufs[0], bufs[1]), n=0) == _lib.IDG_ERR_INVALID_ARGUMENT
+    # cycle 1 names rows past its nr_rows
+    assert run(io(bufs[0], bufs[1]), io(bufs[0], bufs[1], nr_rows=12)) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert "cycle 1: plan entry 1" in _lib.last_error()
+    # cycle 1 reads what cycle 0 writes (its output fed back as input)
+    assert run(io(bufs[0], bufs[1]), io(bufs[1], bufs[2])) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert "cycle 1 reads host memory that cycle 0 writes" in _lib.last_error()
+    # ... or a part of it
+    half = bufs[1][rows // 2:]
+    assert run(io(bufs[0], bufs[1]), io(bufs[2], bufs[3]), io(half, bufs[3])) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert "cycle 2 reads host memory that cycle 0 writes" in _lib.last_error()
+    # a NULL array in a later cycle
+    bad = io(bufs[0], bufs[1])
+    bad.uvw = None
+    assert run(io(bufs[0], bufs[1]), bad) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert "cycle 1: NULL host array" in _lib.last_error()
 
 
 def test_python_wrapper_raises(idg):

@@ -563,10 +563,14 @@ def test_host_buffer_cycle_matches_device_steps(idg, chunk, locked):
             hostmem.release(a)
 
 
-def test_host_buffer_cycle_zeroes_rows_no_entry_names(idg):
+@pytest.mark.parametrize("chunk", [L.CHUNKS_AUTO, 5])
+def test_host_buffer_cycle_zeroes_rows_no_entry_names(idg, chunk):
     """A plan that names only some of the rows (every third config-1 subgrid
-    dropped): idg_imaging_cycle writes the degridded rows and zeros exactly in
-    the rows no entry names, whatever the output buffer held before."""
+    dropped, and the first and the last): idg_imaging_cycle writes the
+    degridded rows and zeros exactly in the rows no entry names, whatever the
+    output buffer held before -- in one chunk, and in chunks of 5 subgrids,
+    where unnamed rows lie before the first chunk, between two chunks' rows
+    and after the last chunk."""
     from idg_gb300 import datasets as D
     from idg_gb300 import ops
 
@@ -574,6 +578,7 @@ def test_host_buffer_cycle_zeroes_rows_no_entry_names(idg):
     obs = D.make_observation(spec)
     vis = _vis(spec, seed=43)
     keep = np.arange(spec.n_subgrids) % 3 != 1
+    keep[0] = keep[-1] = False
     md = np.ascontiguousarray(obs.metadata[keep])
     S, G, N = spec.subgrid_size, spec.grid_size, int(keep.sum())
     gs = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
@@ -594,10 +599,72 @@ def test_host_buffer_cycle_zeroes_rows_no_entry_names(idg):
     out_h = np.full(vis.shape, np.nan + 1j * np.nan, np.complex64)
     try:
         t = ops.imaging_cycle(gs, md, obs.uvw, obs.wavenumbers, vis, obs.taper, np.ascontiguousarray(obs.aterms),
-                              out_h, chunk_subgrids=L.CHUNKS_AUTO)
+                              out_h, chunk_subgrids=chunk)
         assert np.all(out_h[~named] == 0)
-        check_rel("host cycle vis, rows named", out_h[named], v_ref.cpu().numpy()[named], TOL)
-        assert t["total_ms"] > 0
+        check_rel(f"host cycle vis, rows named, chunk={chunk}", out_h[named], v_ref.cpu().numpy()[named], TOL)
+        assert t["total_ms"] > 0 and t["end_ms"] == t["total_ms"]
+        assert t["d2h_vis_bytes"] == vis.nbytes
+    finally:
+        ops.release_buffers()
+
+
+@pytest.mark.parametrize("chunk", [0, 5, L.CHUNKS_ADAPTIVE])
+def test_imaging_cycles_equal_single_cycles(idg, chunk):
+    """idg_imaging_cycles over three config-1 cycles with their own
+    visibilities, the second on a plan that names only some rows (different
+    plan and uvw buffers on the device): each cycle's grid and visibilities
+    are those of the device-resident steps on its inputs, although each
+    cycle's copies in ran during the cycle before it.  Then the bench's form:
+    four cycles on one pair of host buffers."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    spec = D.config1()
+    spec.aterm_sigma = 0.05
+    obs = D.make_observation(spec)
+    S, G, N = spec.subgrid_size, spec.grid_size, spec.n_subgrids
+    gs = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    keep = np.arange(N) % 3 != 1
+    keep[0] = False
+    plans = [obs.metadata, np.ascontiguousarray(obs.metadata[keep]), obs.metadata]
+    vis = [_vis(spec, seed=s) for s in (51, 52, 53)]
+    at = np.ascontiguousarray(obs.aterms)
+    refs = []
+    for md, v in zip(plans, vis):
+        d = {k: dev(x) for k, x in dict(md=md, uvw=obs.uvw, k=obs.wavenumbers, vis=v, taper=obs.taper,
+                                        at=obs.aterms).items()}
+        sub = torch.empty((md.shape[0], 4, S, S), dtype=torch.complex64, device="cuda")
+        g = torch.zeros((1, 4, G, G), dtype=torch.complex64, device="cuda")
+        ops.grid_visibilities(gs, d["md"], d["uvw"], d["k"], d["vis"], d["taper"], d["at"], sub, g)
+        vo = torch.zeros_like(d["vis"])
+        ops.degrid_visibilities(gs, d["md"], d["uvw"], d["k"], vo, d["taper"], d["at"], sub, g)
+        torch.cuda.synchronize()
+        refs.append((g.cpu().numpy(), vo.cpu().numpy()))
+    uvw = [obs.uvw.copy() for _ in plans]  # a buffer per cycle
+    outs = [np.full(v.shape, np.nan + 1j * np.nan, np.complex64) for v in vis]
+    grids = [np.zeros((1, 4, G, G), np.complex64) for _ in vis]
+    try:
+        ts = ops.imaging_cycles(gs, list(zip(plans, uvw, vis, outs, grids)), obs.wavenumbers, obs.taper, at,
+                                chunk_subgrids=chunk)
+        for i, ((g_ref, v_ref), md) in enumerate(zip(refs, plans)):
+            named = np.zeros(vis[i].shape[0], bool)
+            b0 = int(md["baseline_offset"][0])
+            for m in md:
+                r = int(m["baseline_offset"]) - b0 + int(m["time_offset"])
+                named[r:r + int(m["nr_timesteps"])] = True
+            check_rel(f"cycles[{i}] grid chunk={chunk}", grids[i], g_ref, TOL)
+            check_rel(f"cycles[{i}] vis chunk={chunk}", outs[i][named], v_ref[named], TOL)
+            assert np.all(outs[i][~named] == 0)
+        assert all(t["total_ms"] > 0 and t["end_ms"] >= t["total_ms"] for t in ts)
+        assert all(a["end_ms"] < b["end_ms"] for a, b in zip(ts, ts[1:]))
+        assert ts[0]["h2d_bytes"] > ts[2]["h2d_bytes"]  # the constants travel with the first cycle only
+        # four cycles on one pair of host buffers: each copies its inputs in
+        # and its results out; the buffer ends with the last cycle's
+        out = np.zeros_like(vis[0])
+        ts = ops.imaging_cycles(gs, [(plans[0], uvw[0], vis[0], out)] * 4, obs.wavenumbers, obs.taper, at,
+                                chunk_subgrids=chunk)
+        check_rel(f"cycles x4 vis chunk={chunk}", out, refs[0][1], TOL)
+        assert all(t["h2d_vis_bytes"] == vis[0].nbytes and t["d2h_vis_bytes"] == vis[0].nbytes for t in ts)
     finally:
         ops.release_buffers()
 
