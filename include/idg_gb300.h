@@ -499,7 +499,9 @@ typedef struct idg_cycle_io {
  * soon as cycle i's gridding has read its visibilities, and so run while
  * cycle i degrids: after the first cycle, the gridding kernels find their
  * visibilities on the device when the host copy rate is at least the
- * visibilities in / (degridding + gridding time).  Because cycle i+1 reads
+ * visibilities in / (degridding + gridding time).  Every cycle but the last
+ * degrids in one chunk; its copy out runs during the next cycle's gridding.
+ * Because cycle i+1 reads
  * its host inputs before cycle i has written its outputs, no cycle may read
  * host memory that an earlier cycle of the call writes (IDG_ERR_INVALID_ARGUMENT;
  * to feed one cycle's output to the next, call idg_imaging_cycle per cycle).

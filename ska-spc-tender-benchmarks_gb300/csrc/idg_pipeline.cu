@@ -295,6 +295,11 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
             r.gch.assign(1, Chunk{0, n, 0, r.io->nr_rows});
             r.dch = r.gch;
         }
+        // Every cycle but the last degrids in one chunk: its copy out runs
+        // during the next cycle's gridding (which leaves the visibilities
+        // out alone), so only the last cycle's copies out need chunks to
+        // overlap its degridder.
+        if (i + 1 < nr_cycles) r.dch.assign(1, Chunk{0, n, 0, r.io->nr_rows});
     }
     int dev = 0;
     IDG_CUDA(cudaGetDevice(&dev));
