@@ -463,7 +463,8 @@ def run_ours(args, rank, world, local_rank):
             e2e_ms = float(tt.item())
         steps_ms = [ends[0]] + [b - a for a, b in zip(ends, ends[1:])]
         e2e = {"value": world * nvis_e2e / (e2e_ms * 1e-3) / 1e6, "unit": "Mvis/s",
-               "h2d_bytes_per_step": int(totals[-1]["h2d_bytes"]), "d2h_bytes_per_step": int(totals[-1]["d2h_bytes"]),
+               "h2d_bytes_per_step": int(np.mean([t["h2d_bytes"] for t in totals])),
+               "d2h_bytes_per_step": int(np.mean([t["d2h_bytes"] for t in totals])),
                "ms_per_step": e2e_ms,
                "api": "idg_imaging_cycles (C ABI) on page-locked host buffers: the K timed steps are K cycles of one "
                       "call, each copying its inputs in and its visibilities out; a cycle's copies in run during "
