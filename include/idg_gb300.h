@@ -508,7 +508,7 @@ typedef struct idg_cycle_io {
  * Cycles may share their input and output buffers.  Each cycle's timing
  * reports its own copies and phases; total_ms runs from its own first copy
  * in, end_ms from the call's.  With IDG_CHUNKS_ADAPTIVE the first cycle sets
- * the ratio for the next call.  At most 65536 cycles per call. */
+ * the ratio for the next call.  At most 4096 cycles per call. */
 IDG_API int idg_imaging_cycles(const idg_params *params, int variant, int64_t nr_cycles, const idg_cycle_io *cycles,
                                const float *wavenumbers, const float *spheroidal, const void *aterms,
                                int64_t chunk_subgrids);

@@ -193,7 +193,9 @@ struct CycleRun {
     int64_t launches = 0, h2d = 0, d2h = 0, h2d_vis = 0, d2h_vis = 0;
 };
 
-constexpr int kMaxCycles = 1 << 16; // cycles of one idg_imaging_cycles call
+// cycles of one idg_imaging_cycles call: each holds its own events (about
+// 70 at ten chunks per phase), created before the first copy is queued
+constexpr int kMaxCycles = 4096;
 
 bool ranges_overlap(const void *a, size_t na, const void *b, size_t nb) {
     if (!a || !b || na == 0 || nb == 0) return false;
