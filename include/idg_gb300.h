@@ -427,10 +427,10 @@ typedef struct idg_cycle_timing {
     int64_t h2d_bytes;
     int64_t d2h_bytes;
     int64_t kernel_launches;
-    /* The visibility copies alone: h2d_vis_ms is the time the copies in took
-     * on their stream, where they run back to back; d2h_vis_ms is the sum of
-     * the durations of the copies out (each starts when its chunk is
-     * degridded).  bytes / ms gives the host copy rate the cycle saw. */
+    /* The visibility copies alone: h2d_vis_ms and d2h_vis_ms are the sums of
+     * the durations of the copies in and out (a copy in starts when the
+     * stream reaches it, a copy out when its chunk is degridded).  bytes / ms
+     * gives the host copy rate the cycle saw. */
     double h2d_vis_ms;
     double d2h_vis_ms;
     int64_t h2d_vis_bytes;
@@ -496,19 +496,19 @@ typedef struct idg_cycle_io {
 /* A run of imaging cycles on host buffers that share the wavenumbers, taper
  * and A-terms (copied in once), each cycle as idg_imaging_cycle runs it, with
  * the same outputs.  Cycle i+1's copies in (plan, uvw, visibilities) start as
- * soon as cycle i's gridding has read its visibilities, and so run while
- * cycle i degrids: after the first cycle, the gridding kernels find their
- * visibilities on the device when the host copy rate is at least the
- * visibilities in / (degridding + gridding time).  Every cycle but the last
- * degrids in one chunk; its copy out runs during the next cycle's gridding.
- * Because cycle i+1 reads
- * its host inputs before cycle i has written its outputs, no cycle may read
- * host memory that an earlier cycle of the call writes (IDG_ERR_INVALID_ARGUMENT;
- * to feed one cycle's output to the next, call idg_imaging_cycle per cycle).
- * Cycles may share their input and output buffers.  Each cycle's timing
- * reports its own copies and phases; total_ms runs from its own first copy
- * in, end_ms from the call's.  With IDG_CHUNKS_ADAPTIVE the first cycle sets
- * the ratio for the next call.  At most 4096 cycles per call. */
+ * soon as cycle i's gridding has started, each chunk of visibilities once
+ * cycle i's gridding has read the rows it overwrites, and so run while cycle
+ * i grids and degrids; cycle i's copies out run while it degrids and while
+ * cycle i+1 grids.  With IDG_CHUNKS_AUTO / IDG_CHUNKS_ADAPTIVE the first
+ * cycle's gridding and the last cycle's degridding have ten chunks, the other
+ * phases four.  Because cycle i+1 reads its host inputs before cycle i has
+ * written its outputs, no cycle may read host memory that an earlier cycle of
+ * the call writes (IDG_ERR_INVALID_ARGUMENT; to feed one cycle's output to
+ * the next, call idg_imaging_cycle per cycle).  Cycles may share their input
+ * and output buffers.  Each cycle's timing reports its own copies and phases;
+ * total_ms runs from its own first copy in, end_ms from the call's.  With
+ * IDG_CHUNKS_ADAPTIVE the first cycle sets the ratio for the next call.  At
+ * most 4096 cycles per call. */
 IDG_API int idg_imaging_cycles(const idg_params *params, int variant, int64_t nr_cycles, const idg_cycle_io *cycles,
                                const float *wavenumbers, const float *spheroidal, const void *aterms,
                                int64_t chunk_subgrids);

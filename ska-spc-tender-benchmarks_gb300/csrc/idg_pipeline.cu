@@ -59,7 +59,7 @@ struct Chunk {
 };
 
 // Subgrid boundaries 0 = b0 < b1 < ... = n.  chunk > 0: equal chunks of that
-// many subgrids; IDG_CHUNKS_AUTO / IDG_CHUNKS_ADAPTIVE: kAutoChunks chunks
+// many subgrids; IDG_CHUNKS_AUTO / IDG_CHUNKS_ADAPTIVE: `pieces` chunks
 // whose sizes grow by `ratio` from one to the next (`growing`) or shrink by
 // it (otherwise), chunks under kMinChunk subgrids merged into their
 // neighbour; anything else: one chunk.  A growing chunk's copy keeps ahead of
@@ -68,12 +68,13 @@ struct Chunk {
 // gridder: at ratio 1.6, copies at 98 GB/s or more suffice).
 constexpr int64_t kMinChunk = 1024;
 constexpr int kAutoChunks = 10;
+constexpr int kRunChunks = 4; // see run_cycles
 constexpr double kAutoRatio = 1.6;
 constexpr double kMinRatio = 1.1;
-std::vector<int64_t> chunk_bounds(int64_t n, int64_t chunk, bool growing, double ratio) {
+std::vector<int64_t> chunk_bounds(int64_t n, int64_t chunk, bool growing, double ratio, int pieces) {
     std::vector<int64_t> b{0};
     if (chunk == IDG_CHUNKS_AUTO || chunk == IDG_CHUNKS_ADAPTIVE) {
-        const int k = kAutoChunks;
+        const int k = pieces;
         double total = 0;
         for (int i = 0; i < k; ++i) total += std::pow(ratio, i);
         double acc = 0;
@@ -185,11 +186,12 @@ struct CycleRun {
     std::vector<std::pair<int64_t, int64_t>> gaps; // rows no entry names
     std::vector<Chunk> gch, dch;
     void *md = nullptr, *uvw = nullptr;
-    cudaEvent_t t_start, md_in, t_grid0, t_grid1, t_deg1, t_end, h2d_v0, h2d_v1;
-    // per gridding chunk: its copies done (h2d_done), its kernels started
-    // after the wait for them (g_go) and ended with its adder (g_end); per
-    // degridding chunk: its kernels done, its copy out bracketed on s_d2h
-    std::vector<cudaEvent_t> h2d_done, g_go, g_end, deg_done, d2h_b, d2h_e;
+    cudaEvent_t t_start, md_in, t_grid0, t_grid1, t_deg1, t_end;
+    // per gridding chunk: its copy in bracketed on s_h2d (h2d_b, h2d_e), its
+    // kernels started after the wait for it (g_go) and ended with its adder
+    // (g_end); per degridding chunk: its kernels done, its copy out
+    // bracketed on s_d2h
+    std::vector<cudaEvent_t> h2d_b, h2d_e, g_go, g_end, deg_done, d2h_b, d2h_e;
     int64_t launches = 0, h2d = 0, d2h = 0, h2d_vis = 0, d2h_vis = 0;
 };
 
@@ -205,11 +207,12 @@ bool ranges_overlap(const void *a, size_t na, const void *b, size_t nb) {
 
 // The cycles of idg_imaging_cycle (one) and idg_imaging_cycles (several),
 // enqueued on the three streams of the cycle buffers.  Cycle i+1's copies in
-// wait only for cycle i's gridding (the last reader of the visibilities in;
-// its plan and uvw go to the other one of two buffers), so they run while
-// cycle i degrids.  Cycle i+1's degridding waits for cycle i's copies out (the
-// visibilities out are one buffer), and its gridding for cycle i's grid copy
-// when there is one.
+// start once cycle i's gridding has started (its plan and uvw go to the other
+// one of two buffers, which cycle i-1 has finished with), each chunk's
+// visibilities once cycle i's gridding chunks that read those rows have
+// ended, so they run while cycle i grids and degrids.  Cycle i+1's degridding
+// waits for cycle i's copies out (the visibilities out are one buffer), and
+// its gridding for cycle i's grid copy when there is one.
 int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const idg_cycle_io *io,
                const float *wavenumbers, const float *spheroidal, const void *aterms, int64_t chunk_subgrids,
                bool single) {
@@ -292,16 +295,19 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
     for (int64_t i = 0; i < nr_cycles; ++i) {
         CycleRun &r = runs[i];
         const int64_t n = r.io->nr_subgrids;
-        if (!make_chunks(chunk_bounds(n, chunk_subgrids, true, ratio), row0[i], row1[i], &r.gch) ||
-            !make_chunks(chunk_bounds(n, chunk_subgrids, false, kAutoRatio), row0[i], row1[i], &r.dch)) {
+        // In a run of cycles, a cycle after the first finds most of its
+        // visibilities on the device (copied while the cycle before it ran),
+        // and a cycle before the last has until the next cycle's degridding to
+        // copy its results out: kRunChunks chunks suffice there, with fewer
+        // partial last waves of the persistent kernels.  The first cycle's
+        // gridding and the last cycle's degridding keep kAutoChunks.
+        const int gp = i == 0 ? kAutoChunks : kRunChunks, dp = i + 1 == nr_cycles ? kAutoChunks : kRunChunks;
+        if (!make_chunks(chunk_bounds(n, chunk_subgrids, true, i == 0 ? ratio : kAutoRatio, gp), row0[i], row1[i],
+                         &r.gch) ||
+            !make_chunks(chunk_bounds(n, chunk_subgrids, false, kAutoRatio, dp), row0[i], row1[i], &r.dch)) {
             r.gch.assign(1, Chunk{0, n, 0, r.io->nr_rows});
             r.dch = r.gch;
         }
-        // Every cycle but the last degrids in one chunk: its copy out runs
-        // during the next cycle's gridding (which leaves the visibilities
-        // out alone), so only the last cycle's copies out need chunks to
-        // overlap its degridder.
-        if (i + 1 < nr_cycles) r.dch.assign(1, Chunk{0, n, 0, r.io->nr_rows});
     }
     int dev = 0;
     IDG_CUDA(cudaGetDevice(&dev));
@@ -349,18 +355,20 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
         }
     } guard{ev};
     for (CycleRun &r : runs) {
-        for (cudaEvent_t *e : {&r.t_start, &r.t_grid0, &r.t_grid1, &r.t_deg1, &r.t_end, &r.h2d_v0, &r.h2d_v1})
+        for (cudaEvent_t *e : {&r.t_start, &r.t_grid0, &r.t_grid1, &r.t_deg1, &r.t_end})
             if (int rc = new_event(e, true)) return rc;
         if (int rc = new_event(&r.md_in, false)) return rc;
         const size_t ng = r.gch.size(), nd = r.dch.size();
-        r.h2d_done.resize(ng);
+        r.h2d_b.resize(ng);
+        r.h2d_e.resize(ng);
         r.g_go.resize(ng);
         r.g_end.resize(ng);
         r.deg_done.resize(nd);
         r.d2h_b.resize(nd);
         r.d2h_e.resize(nd);
         for (size_t i = 0; i < ng; ++i) {
-            if (int rc = new_event(&r.h2d_done[i], false)) return rc;
+            if (int rc = new_event(&r.h2d_b[i], true)) return rc;
+            if (int rc = new_event(&r.h2d_e[i], true)) return rc;
             if (int rc = new_event(&r.g_go[i], true)) return rc;
             if (int rc = new_event(&r.g_end[i], true)) return rc;
         }
@@ -393,9 +401,11 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
         const CycleRun *prev = ci > 0 ? &runs[ci - 1] : nullptr;
         const idg_cycle_io &c = *r.io;
         const int64_t nr_rows = c.nr_rows;
-        // copies in: after the previous cycle's gridding has read the
-        // visibilities in; the constants once, before the first plan
-        if (prev) IDG_CUDA(cudaStreamWaitEvent(B.s_h2d, prev->t_grid1, 0));
+        // copies in: the constants once, before the first plan; a later
+        // cycle's after the previous cycle's gridding has started, and each
+        // chunk's visibilities after the previous cycle's gridding chunks
+        // that read the rows they overwrite
+        if (prev) IDG_CUDA(cudaStreamWaitEvent(B.s_h2d, prev->t_grid0, 0));
         IDG_CUDA(cudaEventRecord(r.t_start, B.s_h2d));
         if (!prev) {
             IDG_CUDA(cudaMemcpyAsync(B.k, wavenumbers, b_k, cudaMemcpyHostToDevice, B.s_h2d));
@@ -407,7 +417,7 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
         IDG_CUDA(cudaMemcpyAsync(r.md, c.metadata, md_bytes, cudaMemcpyHostToDevice, B.s_h2d));
         r.h2d += md_bytes;
         IDG_CUDA(cudaEventRecord(r.md_in, B.s_h2d));
-        IDG_CUDA(cudaEventRecord(r.h2d_v0, B.s_h2d));
+        int64_t waited = -1; // the previous cycle's last gridding chunk waited for
         for (size_t i = 0; i < r.gch.size(); ++i) {
             const Chunk &k = r.gch[i];
             // uvw: this chunk's rows, with any rows before them that no chunk
@@ -419,15 +429,25 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
                                          (size_t)(u1 - u0) * 12, cudaMemcpyHostToDevice, B.s_h2d));
                 r.h2d += (u1 - u0) * 12;
             }
+            if (prev) {
+                // the previous cycle's chunks are in row order: the last one
+                // starting before this chunk's rows end is the last reader
+                int64_t last = -1;
+                for (size_t q = 0; q < prev->gch.size() && prev->gch[q].r0 < k.r1; ++q) last = (int64_t)q;
+                if (last > waited) {
+                    IDG_CUDA(cudaStreamWaitEvent(B.s_h2d, prev->g_end[last], 0));
+                    waited = last;
+                }
+            }
             const size_t off = (size_t)k.r0 * row_bytes, bytes = (size_t)(k.r1 - k.r0) * row_bytes;
+            IDG_CUDA(cudaEventRecord(r.h2d_b[i], B.s_h2d));
             IDG_CUDA(cudaMemcpyAsync(static_cast<char *>(B.vis_in) + off,
                                      static_cast<const char *>(c.visibilities_in) + off, bytes,
                                      cudaMemcpyHostToDevice, B.s_h2d));
+            IDG_CUDA(cudaEventRecord(r.h2d_e[i], B.s_h2d));
             r.h2d += bytes;
             r.h2d_vis += bytes;
-            IDG_CUDA(cudaEventRecord(r.h2d_done[i], B.s_h2d));
         }
-        IDG_CUDA(cudaEventRecord(r.h2d_v1, B.s_h2d));
 
         // gridding phase (after the previous cycle's grid copy, if any: the
         // grid is zeroed here)
@@ -437,7 +457,7 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
         IDG_CUDA(cudaEventRecord(r.t_grid0, B.s_compute));
         const idg_metadata *d_md = static_cast<const idg_metadata *>(r.md);
         for (size_t i = 0; i < r.gch.size(); ++i) {
-            IDG_CUDA(cudaStreamWaitEvent(B.s_compute, r.h2d_done[i], 0));
+            IDG_CUDA(cudaStreamWaitEvent(B.s_compute, r.h2d_e[i], 0));
             IDG_CUDA(cudaEventRecord(r.g_go[i], B.s_compute));
             const int64_t s0 = r.gch[i].s0, n = r.gch[i].s1 - s0;
             if (int rc = idg_grid_visibilities(params, variant, n, d_md + s0, nullptr, nr_rows,
@@ -499,12 +519,17 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
     }
     for (int64_t ci = 0; ci < nr_cycles; ++ci) {
         const CycleRun &r = runs[ci];
-        float total = 0, g = 0, d = 0, hv = 0, end = 0;
+        float total = 0, g = 0, d = 0, end = 0;
         IDG_CUDA(cudaEventElapsedTime(&total, r.t_start, r.t_end));
         IDG_CUDA(cudaEventElapsedTime(&end, runs[0].t_start, r.t_end));
         IDG_CUDA(cudaEventElapsedTime(&g, r.t_grid0, r.t_grid1));
         IDG_CUDA(cudaEventElapsedTime(&d, r.t_grid1, r.t_deg1));
-        IDG_CUDA(cudaEventElapsedTime(&hv, r.h2d_v0, r.h2d_v1));
+        double hv = 0; // the visibility copies in alone
+        for (size_t i = 0; i < r.gch.size(); ++i) {
+            float x = 0;
+            IDG_CUDA(cudaEventElapsedTime(&x, r.h2d_b[i], r.h2d_e[i]));
+            hv += x;
+        }
         // the gridding kernels' waits for their copies: before the first chunk
         // (after the grid was zeroed) and between one chunk's end and the next's start
         double wait = 0;

@@ -513,6 +513,56 @@ def test_host_buffer_cycle_auto_chunks(idg):
     ops.release_buffers()
 
 
+@pytest.mark.parametrize("mode", [L.CHUNKS_AUTO, L.CHUNKS_ADAPTIVE])
+def test_imaging_cycles_config2_chunked(idg, mode):
+    """Three cycles of one idg_imaging_cycles call on 8192 config-2 subgrids,
+    inputs A, B, A with outputs of their own: each chunk of a cycle's
+    visibilities is copied in once the previous cycle's gridding chunks that
+    read those rows have ended, while that cycle still grids its later chunks.
+    Every cycle's grid and visibilities equal the device-resident steps on its
+    own inputs (a copy that overwrote rows still to be gridded would mix B into
+    A's grid).  Chunks: ten for the first gridding and the last degridding,
+    four elsewhere (fewer where chunks under 1024 subgrids merge)."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    spec = D.config2()
+    obs = D.truncate_observation(D.make_observation(spec), 8192)
+    spec = obs.spec
+    S, G, N = spec.subgrid_size, spec.grid_size, spec.n_subgrids
+    gs = spec_for(G, S, spec.nchannels, spec.nstations, obs.aterms.shape[0], spec.image_size)
+    d = {k: dev(v) for k, v in dict(md=obs.metadata, uvw=obs.uvw, k=obs.wavenumbers, taper=obs.taper,
+                                    at=obs.aterms).items()}
+    sub = torch.empty((N, 4, S, S), dtype=torch.complex64, device="cuda")
+    vis_h, refs = [], []
+    for seed in (61, 62):
+        vis_d = D.visibilities(spec, device="cuda", seed=seed)
+        g = torch.zeros((1, 4, G, G), dtype=torch.complex64, device="cuda")
+        ops.grid_visibilities(gs, d["md"], d["uvw"], d["k"], vis_d, d["taper"], d["at"], sub, g)
+        vo = torch.zeros_like(vis_d)
+        ops.degrid_visibilities(gs, d["md"], d["uvw"], d["k"], vo, d["taper"], d["at"], sub, g)
+        torch.cuda.synchronize()
+        vis_h.append(vis_d.cpu().numpy())
+        refs.append((g.cpu().numpy(), vo.cpu().numpy()))
+        del vis_d, vo, g
+    order = [0, 1, 0]
+    outs = [np.zeros_like(vis_h[0]) for _ in order]
+    grids = [np.zeros((1, 4, G, G), np.complex64) for _ in order]
+    try:
+        ts = ops.imaging_cycles(gs, [(obs.metadata, obs.uvw, vis_h[o], outs[i], grids[i]) for i, o in enumerate(order)],
+                                obs.wavenumbers, obs.taper, np.ascontiguousarray(obs.aterms), chunk_subgrids=mode)
+        for i, o in enumerate(order):
+            t = ts[i]
+            print(f"[cycles] {i}: {t['grid_chunks']} + {t['degrid_chunks']} chunks, gridding waited "
+                  f"{t['gridding_wait_ms']:.2f} of {t['gridding_ms']:.2f} ms, ends at {t['end_ms']:.1f} ms")
+            check_rel(f"cycles config2 [{i}] grid", grids[i], refs[o][0], TOL)
+            check_rel(f"cycles config2 [{i}] vis", outs[i], refs[o][1], TOL)
+            assert t["h2d_vis_bytes"] == vis_h[0].nbytes and t["d2h_vis_bytes"] == vis_h[0].nbytes
+        assert ts[0]["grid_chunks"] > ts[1]["grid_chunks"] >= 2 and ts[2]["degrid_chunks"] > ts[1]["degrid_chunks"] >= 2
+    finally:
+        ops.release_buffers()
+
+
 @pytest.mark.parametrize("chunk", [0, 5, -1, -2])
 @pytest.mark.parametrize("locked", [False, True])
 def test_host_buffer_cycle_matches_device_steps(idg, chunk, locked):
