@@ -482,6 +482,8 @@ def run_ours(args, rank, world, local_rank):
                "chunks": {"gridding": int(totals[-1]["grid_chunks"]), "degridding": int(totals[-1]["degrid_chunks"])},
                "chunk_ratio": round(totals[0]["chunk_ratio"], 3),
                "gridding_wait_ms_steps": [round(t["gridding_wait_ms"], 1) for t in totals],
+               "h2d_ms_steps": [round(t["h2d_vis_ms"], 1) for t in totals],
+               "h2d_span_ms_steps": [round(t["h2d_span_ms"], 1) for t in totals],
                "gridding_ms": float(np.mean([t["gridding_ms"] for t in totals])),
                "degridding_ms": float(np.mean([t["degridding_ms"] for t in totals])),
                "steps_ms": [round(x, 1) for x in steps_ms],
@@ -492,7 +494,10 @@ def run_ours(args, rank, world, local_rank):
                                 "steps_ms": [round(t["total_ms"], 1) for t in singles],
                                 "h2d_gbs_steps": [gbs(t, "h2d") for t in singles],
                                 "chunk_ratio_steps": [round(t["chunk_ratio"], 3) for t in singles],
-                                "gridding_wait_ms_steps": [round(t["gridding_wait_ms"], 1) for t in singles]}}
+                                "gridding_wait_ms_steps": [round(t["gridding_wait_ms"], 1) for t in singles],
+                                "gridding_ms_steps": [round(t["gridding_ms"], 1) for t in singles],
+                                "h2d_ms_steps": [round(t["h2d_vis_ms"], 1) for t in singles],
+                                "h2d_span_ms_steps": [round(t["h2d_span_ms"], 1) for t in singles]}}
         # free the cycle's device buffers and the e2e inputs (vis_host stays for the CPU baseline)
         ops.release_buffers()
         for a in small:

@@ -444,6 +444,10 @@ typedef struct idg_cycle_timing {
     /* From the call's first copy in to the end of this cycle's copies out
      * (idg_imaging_cycles; for idg_imaging_cycle it equals total_ms). */
     double end_ms;
+    /* From this cycle's first copy in to the end of its last visibility copy
+     * in: beside h2d_vis_ms, the time its copy stream spent on other copies
+     * (plan, uvw, constants) or waiting. */
+    double h2d_span_ms;
 } idg_cycle_timing;
 
 /* chunk_subgrids of idg_imaging_cycle: chunks sized for the copy pipeline */

@@ -519,8 +519,9 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
     }
     for (int64_t ci = 0; ci < nr_cycles; ++ci) {
         const CycleRun &r = runs[ci];
-        float total = 0, g = 0, d = 0, end = 0;
+        float total = 0, g = 0, d = 0, end = 0, span = 0;
         IDG_CUDA(cudaEventElapsedTime(&total, r.t_start, r.t_end));
+        IDG_CUDA(cudaEventElapsedTime(&span, r.t_start, r.h2d_e.back()));
         IDG_CUDA(cudaEventElapsedTime(&end, runs[0].t_start, r.t_end));
         IDG_CUDA(cudaEventElapsedTime(&g, r.t_grid0, r.t_grid1));
         IDG_CUDA(cudaEventElapsedTime(&d, r.t_grid1, r.t_deg1));
@@ -574,6 +575,7 @@ int run_cycles(const idg_params *params, int variant, int64_t nr_cycles, const i
         timing->chunk_ratio =
             (chunk_subgrids == IDG_CHUNKS_AUTO || chunk_subgrids == IDG_CHUNKS_ADAPTIVE) ? ratio : 0.0;
         timing->end_ms = end;
+        timing->h2d_span_ms = span;
     }
     return IDG_OK;
 }

@@ -106,6 +106,7 @@ class IdgCycleTiming(ctypes.Structure):
         ("gridding_wait_ms", ctypes.c_double),
         ("chunk_ratio", ctypes.c_double),
         ("end_ms", ctypes.c_double),
+        ("h2d_span_ms", ctypes.c_double),
     ]
 
 
