@@ -513,6 +513,47 @@ def test_host_buffer_cycle_auto_chunks(idg):
     ops.release_buffers()
 
 
+def test_imaging_cycles_of_different_sizes(idg):
+    """One idg_imaging_cycles call over config-1 observations of 14, 28 and 7
+    subgrids (rows 896, 1792, 448): device buffers sized by the largest cycle,
+    the plan and uvw of alternate cycles in alternate buffers; each cycle
+    equals the device-resident steps on its own inputs, in chunks of 5."""
+    from idg_gb300 import datasets as D
+    from idg_gb300 import ops
+
+    spec = D.config1()
+    spec.aterm_sigma = 0.05
+    full = D.make_observation(spec)
+    S, G = spec.subgrid_size, spec.grid_size
+    gs = spec_for(G, S, spec.nchannels, spec.nstations, full.aterms.shape[0], spec.image_size)
+    at = np.ascontiguousarray(full.aterms)
+    cycles, refs = [], []
+    for n, seed in ((14, 71), (28, 72), (7, 73)):
+        obs = D.truncate_observation(full, n)
+        vis = _vis(obs.spec, seed=seed)
+        assert obs.metadata.shape[0] == n and vis.shape[0] == obs.uvw.shape[0]
+        d = {k: dev(x) for k, x in dict(md=obs.metadata, uvw=obs.uvw, k=obs.wavenumbers, vis=vis, taper=obs.taper,
+                                        at=obs.aterms).items()}
+        sub = torch.empty((n, 4, S, S), dtype=torch.complex64, device="cuda")
+        g = torch.zeros((1, 4, G, G), dtype=torch.complex64, device="cuda")
+        ops.grid_visibilities(gs, d["md"], d["uvw"], d["k"], d["vis"], d["taper"], d["at"], sub, g)
+        vo = torch.zeros_like(d["vis"])
+        ops.degrid_visibilities(gs, d["md"], d["uvw"], d["k"], vo, d["taper"], d["at"], sub, g)
+        torch.cuda.synchronize()
+        refs.append((g.cpu().numpy(), vo.cpu().numpy()))
+        cycles.append((obs.metadata, obs.uvw, vis, np.full(vis.shape, np.nan + 1j * np.nan, np.complex64),
+                       np.zeros((1, 4, G, G), np.complex64)))
+    try:
+        ts = ops.imaging_cycles(gs, cycles, full.wavenumbers, full.taper, at, chunk_subgrids=5)
+        for i, ((g_ref, v_ref), c) in enumerate(zip(refs, cycles)):
+            check_rel(f"cycles of sizes [{i}] grid", c[4], g_ref, TOL)
+            check_rel(f"cycles of sizes [{i}] vis", c[3], v_ref, TOL)
+            assert ts[i]["h2d_vis_bytes"] == c[2].nbytes and ts[i]["d2h_vis_bytes"] == c[2].nbytes
+            assert ts[i]["h2d_vis_ms"] > 0 and ts[i]["h2d_span_ms"] >= ts[i]["h2d_vis_ms"] - 0.01
+    finally:
+        ops.release_buffers()
+
+
 @pytest.mark.parametrize("mode", [L.CHUNKS_AUTO, L.CHUNKS_ADAPTIVE])
 def test_imaging_cycles_config2_chunked(idg, mode):
     """Three cycles of one idg_imaging_cycles call on 8192 config-2 subgrids,
