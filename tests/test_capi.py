@@ -118,6 +118,9 @@ def test_imaging_cycles_argument_errors_before_device_work(idg):
 
     assert lib.idg_imaging_cycles(ctypes.byref(p), 0, 1, None, None, None, None, 0) == _lib.IDG_ERR_INVALID_ARGUMENT
     assert run(io(bufs[0], bufs[1]), n=0) == _lib.IDG_ERR_INVALID_ARGUMENT
+    # more cycles than one call takes (checked before the array is read)
+    assert run(io(bufs[0], bufs[1]), n=4097) == _lib.IDG_ERR_INVALID_ARGUMENT
+    assert "nr_cycles outside [1, 4096]" in _lib.last_error()
     # cycle 1 names rows past its nr_rows
     assert run(io(bufs[0], bufs[1]), io(bufs[0], bufs[1], nr_rows=12)) == _lib.IDG_ERR_INVALID_ARGUMENT
     assert "cycle 1: plan entry 1" in _lib.last_error()
